@@ -1,0 +1,380 @@
+"""Benchmark: batched persistent kernel vs one plain launch per simulation.
+
+Workload (one step): 64 DS simulations {Al, Si, Cu, Au} x E0 {5, 10, 20, 30}
+keV x tilt {0, 20, 45, 70} deg, Emin 1 keV, Wc 100 eV, tol_E = tol_W = 1e-3,
+num_el = round(10^U[3,6]) drawn from numpy.random.default_rng(0) in that
+nested order (8,927,966 electrons).  A step transports every electron to
+its end: the persistent kernel runs the whole batch in one launch; the plain
+path makes 64 launches of one thread per electron.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mcd|reference]
+
+Prints one JSON line (rank 0).  Under torchrun each rank runs the whole
+workload on its own electron indices (weak scaling, no data-path collective;
+the ranks only meet at the timing barrier).  --impl reference times the CPU
+restatement of the reference (the C oracle) on all host cores over a bounded
+sample of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "mc-discrete_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+MATERIALS = ("Al", "Si", "Cu", "Au")
+ENERGIES = (5000.0, 10000.0, 20000.0, 30000.0)
+TILTS = (0.0, 20.0, 45.0, 70.0)
+N_SHELLS = {"Al": 3, "Si": 3, "Cu": 4, "Au": 8}
+# Algorithmic work per DS event (inline cross sections for 3 + n_shells
+# channels, channel pick, step, move, angle, quaternion update): FP32 FLOP
+# (FMA = 2) and special-function (MUFU) operations.
+FLOP_PER_EVENT = {k: 176 + 18 * n for k, n in N_SHELLS.items()}   # Si 230, Au 320
+MUFU_PER_EVENT = {k: 17 + 4 * n for k, n in N_SHELLS.items()}     # Si 29, Au 49
+CPU_SAMPLE_PER_SIM = 600
+
+
+def workload():
+    rng = np.random.default_rng(0)
+    sims = []
+    for m in MATERIALS:
+        for E0 in ENERGIES:
+            for t in TILTS:
+                n = int(round(10 ** rng.uniform(3, 6)))
+                sims.append(dict(material=m, E0=E0, Emin=1000.0, s_tilt=t, Wc=100.0, tol_E=1e-3, tol_W=1e-3,
+                                 mode="DS", num_el=n))
+    return sims
+
+
+WORKLOAD_NAME = ("64 DS sims {Al,Si,Cu,Au} x E0 {5,10,20,30} keV x tilt {0,20,45,70} deg, Emin 1 keV, "
+                 "Wc 100 eV, tol 1e-3, num_el round(10^U[3,6]) rng(0)")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of the SM clock and throttle reasons."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(sims, per_sim, steps=1, seed=0):
+    """The C oracle over min(num_el, per_sim) electrons of every simulation."""
+    import coracle
+    import mcd_oracle as O
+    from mcd import _lib, tables
+    threads = os.cpu_count() or 1
+    prepared = []
+    for k, s in enumerate(sims):
+        mat = O.Material(s["material"])
+        m = _lib.material(s["material"])
+        ht = [coracle.HostTable.build(kind, mat, *tables.find_grids(kind, m, s["E0"], s["Emin"], s["Wc"],
+                                                                     s["tol_E"], s["tol_W"]))
+              for kind in ("Moller", "Gryz")]
+        prepared.append((mat, ht, min(per_sim, s["num_el"])))
+    times, events, electrons = [], 0, 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ev = el = 0
+        for k, (s, (mat, ht, n)) in enumerate(zip(sims, prepared)):
+            r = coracle.run(mat, s["E0"], s["Emin"], s["s_tilt"], n, seed=seed, mode="DS", Wc=s["Wc"],
+                            tables=ht, sim_id=k, nthreads=threads)
+            ev += int(r["n_events"].sum())
+            el += n
+        times.append(time.perf_counter() - t0)
+        events, electrons = ev, el
+    return {"times": times, "events": events, "electrons": electrons, "threads": threads}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sims = workload()
+    # warm-up steps run a smaller slice of the same sample
+    if args.warmup:
+        cpu_sample(sims[:4], CPU_SAMPLE_PER_SIM // 4, steps=args.warmup)
+    r = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=args.steps)
+    t = sum(r["times"])
+    v = r["events"] * len(r["times"]) / t
+    sample = ("min(num_el, %d) electrons of each of the 64 sims (%d electrons, %d events per step)"
+              % (CPU_SAMPLE_PER_SIM, r["electrons"], r["events"]))
+    line = {
+        "impl": "reference", "metric": "scatter events/s", "value": v, "unit": "events/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(r["times"]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD_NAME, "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "events/s", "cores": r["threads"], "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "electrons_per_s": r["electrons"] * len(r["times"]) / t,
+        "note": "C restatement of the reference's DS trajectory loop (oracle/mcd_oracle.c), FP64, all host "
+                "threads; the reference itself is Python and is not present on the GPU host",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_mcd(args):
+    import torch
+    from mcd import _lib, engine
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    sims = workload()
+    first = rank << 40            # disjoint Philox electron indices per rank
+    tune = _lib.Tune(args.block, args.blocks_per_sm, args.refill, 0, 0)
+
+    batch = engine.Batch(sims, seed=args.seed, device=dev, first_electron=first)
+    # plain path: one buffer set per simulation, no per-electron output
+    plain = []
+    for k, s in enumerate(sims):
+        mat = _lib.material(s["material"])
+        sim = engine.make_sim(s, s["num_el"], args.seed, first, _lib.FP32, k)
+        bufs = engine.RunBuffers(s["num_el"], _lib.FP32, False, 0, dev)
+        plain.append((sim, mat, batch.tables[2 * (k // len(TILTS)): 2 * (k // len(TILTS)) + 2], bufs))
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def batched_step():
+        batch.zero()
+        batch.launch(tune)
+
+    def plain_step():
+        for sim, mat, tabs, bufs in plain:
+            bufs.zero()
+            engine.launch(sim, mat, tabs, bufs, block_size=args.plain_block)
+
+    def timed(step, k):
+        total = 0.0
+        for _ in range(k):
+            flush.fill_(1.0)                       # evict L2 between timed steps
+            torch.cuda.synchronize(dev)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            total += a.elapsed_time(b) * 1e-3
+        return total
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(args.warmup):
+        batched_step()
+        plain_step()
+    torch.cuda.synchronize(dev)
+    tallies, status = batch.collect()
+    events = sum(t["events"] for t in tallies)
+    electrons = batch.total_electrons
+
+    clocks = ClockSampler(dev.index)
+    barrier()
+    clocks.start()
+    t_batched = timed(batched_step, args.steps)
+    barrier()
+    clk = clocks.stop()
+    t_plain = timed(plain_step, max(1, args.steps // 2))
+    k_plain = max(1, args.steps // 2)
+    ptallies = [engine.collect(b[3]).tally for b in plain]
+    barrier()
+
+    # end to end through the public API: host-side inputs packed and copied
+    # in, tallies copied out to pinned host memory, every step
+    host_t = torch.empty(batch.tallies.shape, dtype=torch.uint8, pin_memory=True)
+    t_e2e = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        batch.prepare()
+        batch.zero()
+        batch.launch(tune)
+        host_t.copy_(batch.tallies, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        t_e2e += time.perf_counter() - t0
+    e2e_tallies = [engine.tally_from_bytes(host_t[k].numpy()) for k in range(batch.n)]
+    assert sum(t["events"] for t in e2e_tallies) == events
+
+    if dist is not None:
+        tt = torch.tensor([t_batched, t_plain, t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_batched, t_plain, t_e2e = tt.tolist()
+        dist.destroy_process_group()
+    if rank != 0:
+        return
+
+    K = args.steps
+    value = events * ws * K / t_batched
+    plain_value = events * ws * k_plain / t_plain
+    # eta: batched vs plain (same counters) and vs the reference's samples
+    zs = []
+    for t, p in zip(tallies, ptallies):
+        n = sum(t[o] for o in ("bks", "abs", "trsm", "long"))
+        zs.append(abs(t["bks"] - p["bks"]) / max(1.0, math.sqrt(max(t["bks"], 1) * (1 - t["bks"] / n))))
+    ref = {}
+    try:
+        S = np.load(os.path.join(ROOT, "tests", "golden", "ref_stats.npz"))
+        for tag, key in (("si10", ("Si", 10000.0, 0.0)), ("cu20t45", ("Cu", 20000.0, 45.0)),
+                         ("al5", ("Al", 5000.0, 0.0))):
+            k = next(i for i, s in enumerate(sims) if (s["material"], s["E0"], s["s_tilt"]) == key)
+            t = tallies[k]
+            n = sum(t[o] for o in ("bks", "abs", "trsm", "long"))
+            ro = S[tag + "/outcome"]
+            k1, n1 = int((ro == 1).sum()), ro.size
+            pp = (k1 + t["bks"]) / (n1 + n)
+            z = abs(k1 / n1 - t["bks"] / n) / math.sqrt(pp * (1 - pp) * (1 / n1 + 1 / n))
+            ref[tag] = {"eta": t["bks"] / n, "eta_reference": k1 / n1, "z": z}
+    except (OSError, KeyError, StopIteration):
+        ref = None
+
+    # roofline: FP32 issue (FLOP) and special-function (MUFU) rates
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    peaks = measured_peaks()
+    fmax = float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+    flop = sum(t["events"] * FLOP_PER_EVENT[s["material"]] for t, s in zip(tallies, sims))
+    mufu = sum(t["events"] * MUFU_PER_EVENT[s["material"]] for t, s in zip(tallies, sims))
+    kt = t_batched / K
+    fp32_peak = sms * 128 * 2 * fmax / 1e12
+    mufu_peak = sms * 16 * fmax / 1e12
+    ach = flop / kt / 1e12
+    ach_mufu = mufu / kt / 1e12
+
+    cpu = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=1, seed=args.seed)
+    cpu_v = cpu["events"] / cpu["times"][0]
+
+    line = {
+        "metric": "scatter events/s", "value": value, "unit": "events/s", "n_gpus": ws, "steps": K,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_batched / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "sims": len(sims), "electrons_per_step": electrons * ws,
+                   "events_per_step": events * ws, "tune": {"block": args.block, "refill": args.refill,
+                                                            "blocks_per_sm": args.blocks_per_sm},
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
+        "electrons_per_s": electrons * ws * K / t_batched,
+        "plain": {"value": plain_value, "unit": "events/s", "ms_per_step": 1e3 * t_plain / k_plain,
+                  "launches_per_step": len(sims)},
+        "batched_over_plain": value / plain_value,
+        "eta": {"batched_vs_plain_max_z": max(zs), "vs_reference": ref},
+        "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": batch.ws_bytes,
+                "d2h_bytes_per_step": int(batch.tallies.numel())},
+        "roofline": {"bound": "fp32-issue", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": ach / fp32_peak, "traffic": None,
+                     "mufu": {"achieved": ach_mufu, "peak": mufu_peak, "unit": "Tops/s", "frac": ach_mufu / mufu_peak},
+                     "peak_note": "nominal %d SMs x 128 FP32 lanes x 2 (MUFU: x16) at sm_max_mhz %.0f" % (sms, fmax / 1e6)},
+        "cpu_baseline": {"value": cpu_v, "unit": "events/s", "cores": cpu["threads"], "kind": "port",
+                         "sample": "C oracle, min(num_el, %d) electrons of each sim (%d events)"
+                                   % (CPU_SAMPLE_PER_SIM, cpu["events"])},
+        "clocks": clk,
+        "gpu_launches": K,
+        "status": status,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mcd", choices=("mcd", "reference"))
+    ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--refill", type=int, default=1)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--plain-block", type=int, default=128)
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mcd(args)
+
+
+if __name__ == "__main__":
+    main()

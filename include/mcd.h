@@ -1,0 +1,241 @@
+/*
+ * mcd.h - C ABI of the GB300 electron-trajectory Monte Carlo (libmcd.so).
+ *
+ * Plain C types only: host structs carry device pointers, every device
+ * buffer is owned by the caller, and every call that touches the GPU is
+ * ordered on the stream it is given (a cudaStream_t passed as void*; NULL is
+ * the legacy default stream).  Calls return an MCD_* code and never trap;
+ * conditions found on the device are OR-ed into a caller-owned status word.
+ *
+ * Each entry point names the reference interface it replaces
+ * (elena-pascal/MC-discrete, paths relative to that project).
+ */
+#ifndef MCD_H
+#define MCD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCD_ABI_VERSION 1
+#define MCD_MAX_SHELLS 8
+#define MCD_MAX_CHANNELS 16
+#define MCD_HIST_E_MAX 256
+#define MCD_HIST_T_MAX 180
+
+/* ---- return codes ------------------------------------------------------ */
+enum {
+    MCD_OK = 0,
+    MCD_EINVAL = 1,     /* bad argument (null pointer, bad enum, bad size)    */
+    MCD_ECUDA = 2,      /* a CUDA runtime call failed                          */
+    MCD_ETOOBIG = 3,    /* a size is beyond a documented limit                 */
+    MCD_ENOSPECIES = 4, /* unknown material name                               */
+    MCD_ENODEV = 5      /* no usable CUDA device                               */
+};
+
+/* ---- device status flags (OR-ed into the caller's uint32 status word) --- */
+#define MCD_FLAG_TABLE_RANGE 0x01u /* E above a table's last E row: last row used  */
+#define MCD_FLAG_RING_FULL   0x02u /* event records did not fit the ring           */
+#define MCD_FLAG_NAN         0x04u /* binary collision gave a NaN polar angle      */
+#define MCD_FLAG_CLAMPED     0x08u /* continuous: energy loss >= E, clamped to E   */
+#define MCD_FLAG_LONG_PATH   0x10u /* continuous: a step of 1e4 A or more          */
+#define MCD_FLAG_LONG        0x20u /* an electron reached max_scatt                */
+#define MCD_FLAG_PARKED      0x40u /* batched: electrons left in flight (budget)   */
+
+/* ---- enums --------------------------------------------------------------- */
+enum { MCD_OUT_NONE = 0, MCD_OUT_BKS = 1, MCD_OUT_ABS = 2, MCD_OUT_TRSM = 3,
+       MCD_OUT_TRDF = 4, MCD_OUT_LONG = 5 };
+/* channels: Rutherford, Moller, Quinn, then Gryzinski shell k = 3 + k in the
+ * material's shell order (MC/tools/scattering.py:483-508)                   */
+enum { MCD_CH_RUTH = 0, MCD_CH_MOLLER = 1, MCD_CH_QUINN = 2, MCD_CH_GRYZ0 = 3 };
+enum { MCD_MODE_DS = 0, MCD_MODE_CONT = 1 };
+enum { MCD_BETHE_CLASSICAL = 0, MCD_BETHE_JL = 1, MCD_BETHE_EXPLICIT = 2 };
+enum { MCD_FP32 = 0, MCD_FP64 = 1 };
+enum { MCD_TABLE_MOLLER = 0, MCD_TABLE_GRYZ = 1 };
+
+/* Reference behaviours that can be switched off (set = reference).          */
+#define MCD_Q_CROSSING_STEP 0x1u /* the step that leaves the sample still loses
+                                    energy, so it can add an 'abs' row
+                                    (MC/tools/singleScatter.py:35-41)        */
+#define MCD_Q_HALF_PHI_FOLD 0x2u /* cos(halfPhi) = +sqrt(1-sin^2)
+                                    (MC/tools/electron.py:90-91)             */
+#define MCD_Q_NAN_DIRECTION 0x4u /* W > (E-Ef)/2 gives NaN cos^2(theta/2);
+                                    off: no deflection for that event
+                                    (MC/tools/scattering.py:177-179)         */
+#define MCD_QUIRKS_REFERENCE 0x7u
+
+/* Optional tallies (mcd_sim.tally_flags).                                     */
+#define MCD_TALLY_CHANNELS 0x1u  /* per-channel event counts                  */
+
+/* ---- material (MC/tools/material.py:117-302) ----------------------------- */
+typedef struct mcd_material {
+    char species[8];
+    char name_val[16];
+    char shell_name[MCD_MAX_SHELLS][8];
+    int32_t Z;
+    int32_t n_shells;
+    double n_val;                    /* valence electrons                     */
+    double E_val;                    /* valence binding energy, eV            */
+    double density;                  /* g/cm^3                                */
+    double atwt;                     /* g/mol                                 */
+    double bethe_k;                  /* Joy-Luo k                             */
+    double atnd;                     /* atoms per m^3                         */
+    double plasmon_e;                /* eV                                    */
+    double fermi_e;                  /* eV                                    */
+    double J;                        /* Bethe mean ionisation energy, eV      */
+    double shell_E[MCD_MAX_SHELLS];  /* binding energies, eV                  */
+    double shell_n[MCD_MAX_SHELLS];  /* occupancies                           */
+} mcd_material;
+
+/* ---- sampled CDF table (MC/tools/probTables.py:70-162, 490-535) ---------- */
+typedef struct mcd_table {
+    const float* Es;         /* device, nE energies (float32 linspace)        */
+    const float* Ws;         /* device, nW energy losses (float32 geomspace)  */
+    const float* cdf;        /* device, nE x (nW-1); 0 marks a masked entry   */
+    const int32_t* nvalid;   /* device, nE unmasked counts per row, or NULL   */
+    int32_t nE;
+    int32_t nW;
+} mcd_table;
+
+/* ---- one simulation (the input.file keys, MC/tools/fileTools.py:8-46) ---- */
+typedef struct mcd_sim {
+    int32_t mode;            /* MCD_MODE_*                                    */
+    int32_t bethe_model;     /* MCD_BETHE_* (continuous mode)                 */
+    int32_t precision;       /* MCD_FP32 or MCD_FP64 transport                */
+    uint32_t quirks;         /* MCD_Q_* bits                                  */
+    uint32_t tally_flags;    /* MCD_TALLY_* bits                              */
+    uint32_t sim_id;         /* Philox counter word 3                         */
+    double E0, Emin;         /* eV                                            */
+    double s_tilt;           /* degrees                                       */
+    double Wc;               /* Moller cut-off, eV (DS)                       */
+    double thickness;        /* A; >= 1e30 means semi-infinite                */
+    int64_t max_scatt;
+    int64_t num_el;
+    uint64_t first_electron; /* Philox electron index of electron 0           */
+    uint64_t seed;           /* Philox key                                    */
+    int32_t hist_E_bins;     /* exit-energy histogram of 'bks' electrons      */
+    int32_t hist_T_bins;     /* polar exit-angle histogram (from -z), degrees */
+    double hist_E_width;     /* eV per bin                                    */
+    double hist_T_width;     /* degrees per bin                               */
+    double J_scale;          /* continuous: Bethe J multiplier (1 = reference)*/
+    double n_scale;          /* density multiplier (1 = reference)            */
+} mcd_sim;
+
+/* ---- per-simulation tallies (device, caller zeroes them) ----------------- */
+typedef struct mcd_tally {
+    unsigned long long outcome[8];       /* first row of each electron        */
+    unsigned long long events;           /* scatter events                    */
+    unsigned long long double_rows;      /* 'bks' then 'abs' in one step      */
+    unsigned long long nan_events;
+    unsigned long long clamped;
+    unsigned long long long_path;
+    unsigned long long table_range;
+    unsigned long long channel[MCD_MAX_CHANNELS];
+    double sum_E_bks;                    /* sum of exit energies, eV          */
+    double sum_E2_bks;
+    double sum_steps2;                   /* sum of squared event counts       */
+    double reserved;
+    unsigned long long hist_E[MCD_HIST_E_MAX];
+    unsigned long long hist_T[MCD_HIST_T_MAX];
+} mcd_tally;
+
+/* ---- per-electron rows (MC/tools/electron.py:105-113), all optional ----- */
+typedef struct mcd_electron_out {
+    uint8_t* outcome;        /* first outcome code                            */
+    uint8_t* flags;          /* bit0: a second 'abs' row, bit1: NaN event     */
+    void* final_E;           /* float (MCD_FP32) or double (MCD_FP64), n      */
+    void* dir;               /* 3 x n, SoA (dx..., dy..., dz...)              */
+    void* last_pos;          /* 3 x n, SoA                                    */
+    void* max_z;             /* deepest z reached, n                          */
+    int32_t* n_events;       /* events of the electron, n                     */
+} mcd_electron_out;
+
+/* ---- per-event records (MC/tools/scattering.py:527-679) ------------------ */
+typedef struct mcd_event {
+    uint32_t electron;       /* electron index within the simulation          */
+    uint32_t step_chan;      /* event index << 5 | channel                    */
+    float E;                 /* energy before the event, eV                   */
+    float W;                 /* energy loss, eV                               */
+    float pathl;             /* step length, A                                */
+    float c2;                /* cos^2(theta/2) ('pol_angle')                  */
+    float half_phi;          /* 'az_angle', rad                               */
+    float x, y, z;           /* position at the start of the event, A         */
+} mcd_event;                 /* 40 bytes                                      */
+
+typedef struct mcd_event_ring {
+    mcd_event* rec;                  /* device, capacity records              */
+    unsigned long long capacity;
+    unsigned long long* cursor;      /* device; records reserved so far; the
+                                        ones at index >= capacity are dropped */
+} mcd_event_ring;
+
+/* ---- launch tuning of the batched kernel -------------------------------- */
+typedef struct mcd_tune {
+    int32_t block_size;      /* threads per block (multiple of 32)            */
+    int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid */
+    int32_t refill;          /* idle lanes a warp waits for before it takes
+                                new electrons from the queue (1..32)          */
+    int32_t reserved;
+    int64_t step_budget;     /* 0 = run to completion; else events per lane
+                                before the kernel parks its electrons         */
+} mcd_tune;
+
+/* ====================== host-only entry points ========================== */
+int mcd_abi_version(void);
+const char* mcd_strerror(int code);
+size_t mcd_struct_size(const char* name);   /* layout check for bindings     */
+
+/* Material constants for Al, Si, Cu or Au.
+ * Replaces material(species) (MC/tools/material.py:117-133, 151-302).       */
+int mcd_material_init(const char* species, mcd_material* out);
+
+/* ======================= device entry points ============================ */
+int mcd_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/* Fill one sampled CDF table in FP64 on the GPU: trapezoid steps of
+ * dsigma/dW between consecutive Ws, cumulative sum, normalised by the row
+ * total; intervals above Wmax(E) = (E - Ef)/2 are masked (stored as 0).
+ * kind is MCD_TABLE_MOLLER (valence electrons, Wmin = Wc) or MCD_TABLE_GRYZ
+ * (shell `shell` of the material).  cdf64 and nvalid may be NULL.
+ * Replaces probTable.computeBlock/generate (MC/tools/probTables.py:415-486). */
+int mcd_build_table(int kind, const mcd_material* mat, int shell,
+                    int32_t nE, int32_t nW, const float* Es, const float* Ws,
+                    float* cdf32, double* cdf64, int32_t* nvalid, void* stream);
+
+/* One simulation, one GPU thread per electron, one launch.
+ * Replaces multiTraj_DS / multiTraj_cont (MC/tools/multiScatter.py:66-116,
+ * 171-229) and trajectory_DS / trajectory_cont_cl
+ * (MC/tools/singleScatter.py:10-41, 205-239).  moller/gryz are used in DS
+ * mode only (gryz = the outermost shell's table, which samples every
+ * Gryzinski loss, MC/tools/scattering.py:625).  electrons and ring may be
+ * NULL.  tally and status are device pointers.                              */
+int mcd_run(const mcd_sim* sim, const mcd_material* mat,
+            const mcd_table* moller, const mcd_table* gryz,
+            mcd_tally* tally, const mcd_electron_out* electrons,
+            const mcd_event_ring* ring, uint32_t* status,
+            int32_t block_size, void* stream);
+
+/* Many simulations of uneven size in one persistent launch fed by a global
+ * work queue.  mcd_batch_prepare packs the simulations into a caller-owned
+ * device workspace of mcd_batch_workspace_bytes(nsims) bytes (host-to-device
+ * copy on `stream`; host memory may be reused when the call returns).
+ * mcd_run_batched then only resets the queue and launches, so it can be
+ * captured in a CUDA graph.  tallies[nsims] and status are device pointers.
+ * Replaces MapScatterer.__call__ (MC/doScatter.py:54-95) with its pool of
+ * multiTraj_* jobs.                                                          */
+size_t mcd_batch_workspace_bytes(int32_t nsims);
+int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims,
+                      const mcd_material* mats, const int32_t* sim_material,
+                      const mcd_table* tables, const int32_t* sim_moller,
+                      const int32_t* sim_gryz, void* workspace,
+                      size_t workspace_bytes, void* stream);
+int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallies,
+                    const mcd_tune* tune, uint32_t* status, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCD_H */

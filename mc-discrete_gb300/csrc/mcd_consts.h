@@ -1,0 +1,182 @@
+// mcd_consts.h - per-simulation constant block shared by host and device.
+//
+// All cross sections are folded into inverse-mean-free-path units (1/A):
+// sigma' = n * sigma * 1e-14, so that the step length is -ln(U) / sum(sigma')
+// (MC/tools/scattering.py:19-36: mfp = 1e14 / (n * sum(sigma)) A) and every
+// quantity stays well inside FP32 range.  The algebra below restates the
+// reference formulas in forms that need fewer divisions and no cancellation:
+//
+//  Rutherford (MC/tools/crossSections.py:14-58), alpha = a0 / E,
+//     sigma' = cR * r^2 / (E + a0),  r = (E + 511000) / (E + 1024000),
+//     cR = 5.21e-21 * 1e6 * 4 pi Z^2 / a0 * n * 1e-14,  a0 = 3.4 Z^0.666667
+//  Moller (crossSections.py:183-208), E > Wc,
+//     sigma' = pM / E^2 * (E/Wc - E/(E-Wc) + ln(Wc/(E-Wc))),
+//     pM = n_val * pi e^4 * n * 1e-14
+//  Gryzinski shell k (crossSections.py:213-242), E > Es,
+//     sigma' = gP * x sqrt(x) * (1 + 2/3 (1 - Es/(2E)) ln(2.7 + sqrt((E-Es)/Es))) / E,
+//     x = (E - Es)/(E + Es),  gP = ns * pi e^4 * n * 1e-14 / Es
+//  Quinn (crossSections.py:247-284), E > Epl, a = E/Ef, b = Epl/Ef,
+//     sigma' = qK / E * ln(qC1 * (sqrt(a) + sqrt(a - b)) / b),
+//     qK = 1e-10 * Epl / (2 a_Bohr),  qC1 = sqrt(1 + b) - 1
+//     (sqrt(a) - sqrt(a-b) = b / (sqrt(a) + sqrt(a-b)))
+//  Bethe (MC/tools/stoppingPowers.py:112-215), eV/A,
+//     classical  S = bP / E * ln(1.166 E / J)
+//     JL         S = bP / E * ln(1.166 (E + k J) / J)
+//     explicit   S = bX / E * (bW * ln E - bC),
+//                bW = Zval + sum Zi,  bC = Zval ln Eval + sum Zi ln Ei
+//     bP = 2 pi e^4 n Z 1e-14,  bX = 2 pi e^4 n 1e-14
+#ifndef MCD_CONSTS_H
+#define MCD_CONSTS_H
+
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/mcd.h"
+
+namespace mcd {
+
+constexpr double kPiEfour = 6.51408491409531e-14;  // cm^2 eV^2 (parameters.py:7)
+constexpr double kBohrR = 5.29177210544e-11;       // m (CODATA 2022)
+constexpr double kPi = 3.141592653589793;
+
+struct TableDev {
+    const float* Es;
+    const float* Ws;
+    const float* cdf;
+    const int32_t* nvalid;
+    int32_t nE;
+    int32_t nW;
+};
+
+template <class T>
+struct SimConst {
+    // transport
+    T E0, Emin, thickness;
+    T d0x, d0y, d0z;
+    // Rutherford
+    T cR, a0;
+    // Moller
+    T pM, Wc;
+    // Gryzinski shells
+    T gEs[MCD_MAX_SHELLS];
+    T gP[MCD_MAX_SHELLS];
+    T gInvEs[MCD_MAX_SHELLS];
+    // Quinn
+    T qK, qC1, qInvEf, qB, Epl;
+    // binary collision
+    T Ef;
+    // Bethe
+    T bP, bJ, bInvJ, bkJ, bX, bW, bC;
+    int32_t nsh;
+    int32_t mode;
+    int32_t bethe;
+    uint32_t quirks;
+    uint32_t tally_flags;
+    uint32_t sim_id;
+    uint32_t key0, key1;
+    int64_t max_scatt;
+    uint64_t first;
+    int64_t num_el;
+    int32_t hE, hT;
+    T invWE, invWT;  // 1/bin width (eV, degrees)
+    TableDev tm, tg;
+};
+
+// Host-side builder: precompute the constant block of one simulation.
+template <class T>
+inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
+                               const mcd_table* tm, const mcd_table* tg) {
+    SimConst<T> c;
+    const double n = m.atnd * (s.n_scale > 0 ? s.n_scale : 1.0);
+    const double Z = (double)m.Z;
+    const double t = s.s_tilt * kPi / 180.0;
+    c.E0 = (T)s.E0;
+    c.Emin = (T)s.Emin;
+    c.thickness = (T)(s.thickness > 0 ? s.thickness : 1e30);
+    c.d0x = (T)(-sin(t));
+    c.d0y = (T)0;
+    c.d0z = (T)cos(t);
+    const double a0 = 3.4 * pow(Z, 0.666667);
+    c.a0 = (T)a0;
+    c.cR = (T)(5.21e-21 * 1e6 * 4.0 * kPi * Z * Z / a0 * n * 1e-14);
+    c.pM = (T)(m.n_val * kPiEfour * n * 1e-14);
+    c.Wc = (T)s.Wc;
+    c.nsh = m.n_shells;
+    for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
+        if (k < m.n_shells) {
+            c.gEs[k] = (T)m.shell_E[k];
+            c.gP[k] = (T)(m.shell_n[k] * kPiEfour * n * 1e-14 / m.shell_E[k]);
+            c.gInvEs[k] = (T)(1.0 / m.shell_E[k]);
+        } else {
+            c.gEs[k] = (T)1e30;  // never below E: sigma' = 0
+            c.gP[k] = (T)0;
+            c.gInvEs[k] = (T)0;
+        }
+    }
+    // plasmon and Fermi energies scale with the density
+    const double scale = (s.n_scale > 0 ? s.n_scale : 1.0);
+    const double Epl = m.plasmon_e * sqrt(scale);
+    const double Ef = m.fermi_e * pow(scale, 2.0 / 3.0);
+    const double b = Epl / Ef;
+    c.Epl = (T)Epl;
+    c.Ef = (T)Ef;
+    c.qK = (T)(1e-10 * Epl / (2.0 * kBohrR));
+    c.qC1 = (T)(sqrt(1.0 + b) - 1.0);
+    c.qInvEf = (T)(1.0 / Ef);
+    c.qB = (T)b;
+    const double J = m.J * (s.J_scale > 0 ? s.J_scale : 1.0);
+    c.bP = (T)(2.0 * kPiEfour * n * Z * 1e-14);
+    c.bJ = (T)J;
+    c.bInvJ = (T)(1.0 / J);
+    c.bkJ = (T)(m.bethe_k * J);
+    c.bX = (T)(2.0 * kPiEfour * n * 1e-14);
+    double w = m.n_val, cc = m.n_val * log(m.E_val);
+    for (int k = 0; k < m.n_shells; ++k) {
+        w += m.shell_n[k];
+        cc += m.shell_n[k] * log(m.shell_E[k]);
+    }
+    c.bW = (T)w;
+    c.bC = (T)cc;
+    c.mode = s.mode;
+    c.bethe = s.bethe_model;
+    c.quirks = s.quirks;
+    c.tally_flags = s.tally_flags;
+    c.sim_id = s.sim_id;
+    c.key0 = (uint32_t)(s.seed & 0xffffffffull);
+    c.key1 = (uint32_t)(s.seed >> 32);
+    c.max_scatt = s.max_scatt > 0 ? s.max_scatt : INT64_MAX;
+    c.first = s.first_electron;
+    c.num_el = s.num_el;
+    c.hE = s.hist_E_bins;
+    c.hT = s.hist_T_bins;
+    c.invWE = (T)(s.hist_E_width > 0 ? 1.0 / s.hist_E_width : 0.0);
+    c.invWT = (T)(s.hist_T_width > 0 ? 1.0 / s.hist_T_width : 0.0);
+    TableDev z{nullptr, nullptr, nullptr, nullptr, 0, 0};
+    c.tm = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->nE, tm->nW} : z;
+    c.tg = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->nE, tg->nW} : z;
+    return c;
+}
+
+// Validation shared by the entry points; returns an MCD_* code.
+inline int check_sim(const mcd_sim& s, const mcd_material& m, const mcd_table* tm,
+                     const mcd_table* tg) {
+    if (s.mode != MCD_MODE_DS && s.mode != MCD_MODE_CONT) return MCD_EINVAL;
+    if (s.mode == MCD_MODE_CONT && (s.bethe_model < 0 || s.bethe_model > 2)) return MCD_EINVAL;
+    if (s.precision != MCD_FP32 && s.precision != MCD_FP64) return MCD_EINVAL;
+    if (!(s.E0 > s.Emin) || !(s.Emin > 0)) return MCD_EINVAL;
+    if (s.num_el < 0) return MCD_EINVAL;
+    if (m.n_shells < 0 || m.n_shells > MCD_MAX_SHELLS || m.atnd <= 0) return MCD_EINVAL;
+    if (s.hist_E_bins < 0 || s.hist_E_bins > MCD_HIST_E_MAX) return MCD_ETOOBIG;
+    if (s.hist_T_bins < 0 || s.hist_T_bins > MCD_HIST_T_MAX) return MCD_ETOOBIG;
+    if (s.mode == MCD_MODE_DS) {
+        if (!tm || !tg) return MCD_EINVAL;
+        if (!tm->Es || !tm->Ws || !tm->cdf || tm->nE < 1 || tm->nW < 2) return MCD_EINVAL;
+        if (!tg->Es || !tg->Ws || !tg->cdf || tg->nE < 1 || tg->nW < 2) return MCD_EINVAL;
+        if (!(s.Wc > 0)) return MCD_EINVAL;
+    }
+    return MCD_OK;
+}
+
+}  // namespace mcd
+
+#endif  // MCD_CONSTS_H

@@ -1,0 +1,473 @@
+// mcd_device.cuh - device side of the transport: counter-based random
+// numbers, cross sections, table sampling, the DS and continuous event and
+// the direction update.  One template serves FP32 (throughput) and FP64
+// (parity) transport.
+#ifndef MCD_DEVICE_CUH
+#define MCD_DEVICE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mcd_consts.h"
+
+namespace mcd {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  Counter = (event,
+// electron lo, electron hi, sim id), key = seed: every (sim, electron, event)
+// has its own block of four 32-bit words, so any electron range can be
+// re-run, sharded or recomputed (the adjoint) without stored state.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// precision traits
+// ---------------------------------------------------------------------------
+template <class T>
+struct Ops;
+
+template <>
+struct Ops<float> {
+    // uniform in (0,1) from the top 23 bits, and its exact complement 1 - U
+    static __device__ __forceinline__ float unit(uint32_t u) {
+        return (float)(u >> 9) * 0x1p-23f + 0x1p-24f;
+    }
+    static __device__ __forceinline__ float unit_c(uint32_t u) {
+        return (float)((~u) >> 9) * 0x1p-23f + 0x1p-24f;
+    }
+    static __device__ __forceinline__ float ln(float x) { return __logf(x); }
+    static __device__ __forceinline__ float ln_acc(float x) { return logf(x); }
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ void sincos_pi(float u, float* s, float* c) {
+        __sincosf(3.14159265358979f * u, s, c);
+    }
+    static __device__ __forceinline__ float nan_() { return __int_as_float(0x7fc00000); }
+    static __device__ __forceinline__ float acos_deg(float x) { return acosf(x) * 57.2957795f; }
+};
+
+template <>
+struct Ops<double> {
+    static __device__ __forceinline__ double unit(uint32_t u) { return ((double)u + 0.5) * 0x1p-32; }
+    static __device__ __forceinline__ double unit_c(uint32_t u) { return ((double)(~u) + 0.5) * 0x1p-32; }
+    static __device__ __forceinline__ double ln(double x) { return log(x); }
+    static __device__ __forceinline__ double ln_acc(double x) { return log(x); }
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double rsqrt_(double x) { return 1.0 / sqrt(x); }
+    static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __device__ __forceinline__ void sincos_pi(double u, double* s, double* c) {
+        const double a = 3.141592653589793 * u;
+        *s = sin(a);
+        *c = cos(a);
+    }
+    static __device__ __forceinline__ double nan_() { return __longlong_as_double(0x7ff8000000000000ll); }
+    static __device__ __forceinline__ double acos_deg(double x) { return acos(x) * 57.29577951308232; }
+};
+
+// ---------------------------------------------------------------------------
+// cross sections in 1/A (see mcd_consts.h for the algebra)
+// ---------------------------------------------------------------------------
+template <class T, class C>
+__device__ __forceinline__ T sig_ruth(const C& c, T E) {
+    const T r = Ops<T>::div(E + (T)511000, E + (T)1024000);
+    return Ops<T>::div(c.cR * r * r, E + c.a0);
+}
+
+template <class T, class C>
+__device__ __forceinline__ T sig_moller(const C& c, T E) {
+    const T Wc = c.Wc;
+    if (!(E > Wc)) return (T)0;
+    const T EmW = E - Wc;
+    const T inv = Ops<T>::div((T)1, E * E);
+    return c.pM * inv * (Ops<T>::div(E, Wc) - Ops<T>::div(E, EmW) + Ops<T>::ln(Ops<T>::div(Wc, EmW)));
+}
+
+template <class T, class C>
+__device__ __forceinline__ T sig_gryz(const C& c, T E, int k) {
+    const T Es = c.gEs[k];
+    if (!(E > Es)) return (T)0;
+    const T d = E - Es;
+    const T x = Ops<T>::div(d, E + Es);
+    const T br = (T)1 + (T)(2.0 / 3.0) * ((T)1 - (T)0.5 * Es * Ops<T>::div((T)1, E)) *
+                            Ops<T>::ln((T)2.7 + Ops<T>::sqrt_(d * c.gInvEs[k]));
+    return Ops<T>::div(c.gP[k] * x * Ops<T>::sqrt_(x) * br, E);
+}
+
+template <class T, class C>
+__device__ __forceinline__ T sig_quinn(const C& c, T E) {
+    if (!(E > c.Epl)) return (T)0;
+    const T a = E * c.qInvEf;
+    const T sa = Ops<T>::sqrt_(a), sb = Ops<T>::sqrt_(a - c.qB);
+    return Ops<T>::div(c.qK, E) * Ops<T>::ln(Ops<T>::div(c.qC1 * (sa + sb), c.qB));
+}
+
+template <class T, class C>
+__device__ __forceinline__ T stopping(const C& c, T E) {
+    if (c.bethe == MCD_BETHE_CLASSICAL)
+        return Ops<T>::div(c.bP, E) * Ops<T>::ln((T)1.166 * E * c.bInvJ);
+    if (c.bethe == MCD_BETHE_JL)
+        return Ops<T>::div(c.bP, E) * Ops<T>::ln((T)1.166 * (E + c.bkJ) * c.bInvJ);
+    return Ops<T>::div(c.bX, E) * (c.bW * Ops<T>::ln(E) - c.bC);
+}
+
+// ---------------------------------------------------------------------------
+// table sampling (MC/tools/scattering.py:63-94): the first E row >= E, then
+// the first CDF entry >= U in that row (masked entries, stored as 0, act as
+// +inf); the loss is the lower W grid point Ws[j].
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ int table_row(const TableDev& t, T E, bool* out_of_range) {
+    const int nE = t.nE;
+    const float e0 = __ldg(t.Es), eL = __ldg(t.Es + nE - 1);
+    if (E > (T)eL) {
+        *out_of_range = true;
+        return nE - 1;
+    }
+    if (!(E > (T)e0)) return 0;
+    // linear-grid guess, then an exact correction against the stored values
+    int g = (int)ceil((double)((E - (T)e0) * (T)(nE - 1) / (T)(eL - e0)));
+    g = g < 1 ? 1 : (g > nE - 1 ? nE - 1 : g);
+    int lo = 0, hi = nE - 1;  // invariant: Es[lo] < E <= Es[hi]
+    for (int it = 0; it < 4; ++it) {
+        if ((T)__ldg(t.Es + g) >= E) {
+            hi = g;
+            if ((T)__ldg(t.Es + g - 1) < E) return g;
+            --g;
+        } else {
+            lo = g;
+            ++g;
+        }
+        if (g <= lo || g > hi) break;
+    }
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((T)__ldg(t.Es + mid) >= E) hi = mid; else lo = mid;
+    }
+    return hi;
+}
+
+template <class T>
+__device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) {
+    const int i = table_row(t, E, oor);
+    const int ncol = t.nW - 1;
+    const float* row = t.cdf + (size_t)i * ncol;
+    int lo = 0, hi = t.nvalid ? __ldg(t.nvalid + i) : ncol;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const float v = __ldg(row + mid);
+        if (v != 0.0f && (T)v < U) lo = mid + 1; else hi = mid;
+    }
+    return (T)__ldg(t.Ws + lo);
+}
+
+// ---------------------------------------------------------------------------
+// electron state
+// ---------------------------------------------------------------------------
+enum : uint32_t { F_DOUBLE_ROW = 1u, F_NAN = 2u, F_TABLE_RANGE = 4u, F_CLAMPED = 8u, F_LONG_PATH = 16u };
+
+template <class T>
+struct Lane {
+    T E, x, y, z, dx, dy, dz, yx, yy, yz;
+    T E_row;   // energy of the first outcome row
+    T max_z;
+    int64_t step;
+    uint32_t outcome;
+    uint32_t flags;
+    uint32_t nan_n, clamp_n, lpath_n;
+};
+
+template <class T, class C>
+__device__ __forceinline__ void lane_init(Lane<T>& L, const C& c) {
+    L.E = c.E0;
+    L.x = L.y = L.z = (T)0;
+    L.dx = c.d0x;
+    L.dy = c.d0y;
+    L.dz = c.d0z;
+    L.yx = (T)0;
+    L.yy = (T)1;
+    L.yz = (T)0;
+    L.E_row = c.E0;
+    L.max_z = (T)0;
+    L.step = 0;
+    L.outcome = MCD_OUT_NONE;
+    L.flags = 0;
+    L.nan_n = L.clamp_n = L.lpath_n = 0;
+}
+
+// One event's record, filled when a ring is attached.
+template <class T>
+struct EventOut {
+    T E, W, pathl, c2, half_phi, x, y, z;
+    int ch;
+};
+
+// Position update and the exit tests (MC/tools/electron.py:64-84).
+template <class T, class C>
+__device__ __forceinline__ void lane_move(Lane<T>& L, const C& c, T s) {
+    const T nz = L.z + s * L.dz;
+    if (nz <= (T)0) {
+        L.outcome = MCD_OUT_BKS;
+        L.E_row = L.E;
+    } else if (nz >= c.thickness) {
+        L.outcome = MCD_OUT_TRSM;
+        L.E_row = L.E;
+    } else {
+        L.x += s * L.dx;
+        L.y += s * L.dy;
+        L.z = nz;
+        L.max_z = nz > L.max_z ? nz : L.max_z;
+    }
+}
+
+// Energy update (MC/tools/electron.py:44-59): the 'abs' row keeps the
+// pre-loss energy; after a 'bks' in the same step it is a second row.
+template <class T, class C>
+__device__ __forceinline__ void lane_lose(Lane<T>& L, const C& c, T W) {
+    const T e = L.E - W;
+    if (e <= c.Emin) {
+        if (L.outcome == MCD_OUT_NONE) {
+            L.outcome = MCD_OUT_ABS;
+            L.E_row = L.E;
+        } else if (L.outcome == MCD_OUT_BKS) {
+            L.flags |= F_DOUBLE_ROW;
+        }
+    }
+    L.E = e;
+}
+
+// Direction update (MC/tools/electron.py:87-99, MC/tools/rotation.py:41-53):
+// q = q_az * q_pol with q_pol = (cos t/2, y sin t/2), q_az = (cos h, d sin h),
+// applied to d and y, each renormalised.  s2 = sin^2(theta/2).
+template <class T, class C>
+__device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_phi) {
+    const T st = Ops<T>::sqrt_(s2);
+    const T ct = Ops<T>::sqrt_((T)1 - s2);
+    T sp, cp;
+    Ops<T>::sincos_pi(u_phi, &sp, &cp);
+    if (c.quirks & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
+    const T dy_ = L.dx * L.yx + L.dy * L.yy + L.dz * L.yz;
+    // cross d x y
+    const T cx = L.dy * L.yz - L.dz * L.yy;
+    const T cy = L.dz * L.yx - L.dx * L.yz;
+    const T cz = L.dx * L.yy - L.dy * L.yx;
+    const T w = cp * ct - sp * st * dy_;
+    const T a = cp * st, b = ct * sp, e = sp * st;
+    const T vx = a * L.yx + b * L.dx + e * cx;
+    const T vy = a * L.yy + b * L.dy + e * cy;
+    const T vz = a * L.yz + b * L.dz + e * cz;
+    // p' = p + w t + v x t,  t = 2 v x p
+    T nd[3], ny[3];
+    {
+        const T tx = (T)2 * (vy * L.dz - vz * L.dy);
+        const T ty = (T)2 * (vz * L.dx - vx * L.dz);
+        const T tz = (T)2 * (vx * L.dy - vy * L.dx);
+        nd[0] = L.dx + w * tx + (vy * tz - vz * ty);
+        nd[1] = L.dy + w * ty + (vz * tx - vx * tz);
+        nd[2] = L.dz + w * tz + (vx * ty - vy * tx);
+    }
+    {
+        const T tx = (T)2 * (vy * L.yz - vz * L.yy);
+        const T ty = (T)2 * (vz * L.yx - vx * L.yz);
+        const T tz = (T)2 * (vx * L.yy - vy * L.yx);
+        ny[0] = L.yx + w * tx + (vy * tz - vz * ty);
+        ny[1] = L.yy + w * ty + (vz * tx - vx * tz);
+        ny[2] = L.yz + w * tz + (vx * ty - vy * tx);
+    }
+    const T rd = Ops<T>::rsqrt_(nd[0] * nd[0] + nd[1] * nd[1] + nd[2] * nd[2]);
+    const T ry = Ops<T>::rsqrt_(ny[0] * ny[0] + ny[1] * ny[1] + ny[2] * ny[2]);
+    L.dx = nd[0] * rd;
+    L.dy = nd[1] * rd;
+    L.dz = nd[2] * rd;
+    L.yx = ny[0] * ry;
+    L.yy = ny[1] * ry;
+    L.yz = ny[2] * ry;
+}
+
+// ---------------------------------------------------------------------------
+// DS event (MC/tools/scattering.py:440-679 in the order of
+// MC/tools/singleScatter.py:15-41).  Returns the channel code.
+// ---------------------------------------------------------------------------
+template <class T, bool REC, class C>
+__device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev) {
+    const T E = L.E;
+    // --- 'long' check first (MC/tools/singleScatter.py:19-23)
+    if (L.step >= c.max_scatt) {
+        L.outcome = MCD_OUT_LONG;
+        L.E_row = E;
+        return -1;
+    }
+    const uint4 r = philox(make_uint4((uint32_t)L.step, (uint32_t)elec, (uint32_t)(elec >> 32), c.sim_id),
+                           c.key0, c.key1);
+    L.step += 1;
+    // --- cross sections, channel order Ruth, Moller, Gryz[k], Quinn
+    const T sR = sig_ruth<T>(c, E);
+    const T sM = sig_moller<T>(c, E);
+    T sG[MCD_MAX_SHELLS];
+    T tot = sR + sM;
+#pragma unroll
+    for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
+        sG[k] = (k < c.nsh) ? sig_gryz<T>(c, E, k) : (T)0;
+        tot += sG[k];
+    }
+    const T sQ = sig_quinn<T>(c, E);
+    tot += sQ;
+    // --- channel (MC/tools/scattering.py:39-59)
+    const T target = Ops<T>::unit(r.x) * tot;
+    int ch = MCD_CH_QUINN;
+    T cum = sR;
+    if (target <= cum) {
+        ch = MCD_CH_RUTH;
+    } else {
+        cum += sM;
+        if (target <= cum) {
+            ch = MCD_CH_MOLLER;
+        } else {
+#pragma unroll
+            for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
+                cum += sG[k];
+                if (ch == MCD_CH_QUINN && k < c.nsh && target <= cum) ch = MCD_CH_GRYZ0 + k;
+            }
+        }
+    }
+    // --- path length (MC/tools/scattering.py:551-565)
+    const T s = -Ops<T>::ln_acc(Ops<T>::unit(r.y)) * Ops<T>::div((T)1, tot);
+    const T x0 = L.x, y0 = L.y, z0 = L.z;
+    lane_move(L, c, s);
+    // --- energy loss and polar angle (MC/tools/scattering.py:568-679)
+    T W, s2;
+    if (ch == MCD_CH_RUTH) {
+        const T a = Ops<T>::div(c.a0, E);
+        W = (T)0;
+        s2 = Ops<T>::div(a * Ops<T>::unit(r.z), a + Ops<T>::unit_c(r.z));
+    } else if (ch == MCD_CH_QUINN) {
+        W = c.Epl;
+        s2 = (T)0;
+    } else {
+        bool oor = false;
+        W = table_pick<T>(ch == MCD_CH_MOLLER ? c.tm : c.tg, E, Ops<T>::unit(r.z), &oor);
+        if (oor) L.flags |= F_TABLE_RANGE;
+        // binary collision (MC/tools/scattering.py:156-179)
+        if (W <= (E - c.Ef) * (T)0.5) {
+            const T q = Ops<T>::div(W, E);
+            s2 = (T)0.5 * Ops<T>::div(q, (T)1 + Ops<T>::sqrt_((T)1 - q));
+        } else {
+            L.flags |= F_NAN;
+            L.nan_n += 1;
+            s2 = (c.quirks & MCD_Q_NAN_DIRECTION) ? Ops<T>::nan_() : (T)0;
+        }
+    }
+    const T uphi = Ops<T>::unit(r.w);
+    if (REC) {
+        ev->E = E;
+        ev->W = W;
+        ev->pathl = s;
+        ev->c2 = (T)1 - s2;
+        ev->half_phi = (T)3.141592653589793 * uphi;
+        ev->x = x0;
+        ev->y = y0;
+        ev->z = z0;
+        ev->ch = ch;
+    }
+    const bool left = L.outcome != MCD_OUT_NONE;
+    if (!left || (c.quirks & MCD_Q_CROSSING_STEP)) lane_lose(L, c, W);
+    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
+    return ch;
+}
+
+// ---------------------------------------------------------------------------
+// continuous event (MC/tools/scattering.py:753-883 in the order of
+// MC/tools/singleScatter.py:210-239, with the Bethe law the mode names)
+// ---------------------------------------------------------------------------
+template <class T, bool REC, class C>
+__device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev) {
+    const T E = L.E;
+    if (L.step >= c.max_scatt) {
+        L.outcome = MCD_OUT_LONG;
+        L.E_row = E;
+        return -1;
+    }
+    const uint4 r = philox(make_uint4((uint32_t)L.step, (uint32_t)elec, (uint32_t)(elec >> 32), c.sim_id),
+                           c.key0, c.key1);
+    L.step += 1;
+    const T sR = sig_ruth<T>(c, E);
+    const T s = -Ops<T>::ln_acc(Ops<T>::unit(r.y)) * Ops<T>::div((T)1, sR);
+    if (!(s < (T)1e4)) {
+        L.flags |= F_LONG_PATH;
+        L.lpath_n += 1;
+    }
+    const T x0 = L.x, y0 = L.y, z0 = L.z;
+    lane_move(L, c, s);
+    T dE = s * stopping<T>(c, E);
+    if (!(dE < E)) {
+        L.flags |= F_CLAMPED;
+        L.clamp_n += 1;
+        dE = E;
+    }
+    const T a = Ops<T>::div(c.a0, E);
+    const T s2 = Ops<T>::div(a * Ops<T>::unit(r.z), a + Ops<T>::unit_c(r.z));
+    const T uphi = Ops<T>::unit(r.w);
+    if (REC) {
+        ev->E = E;
+        ev->W = dE;
+        ev->pathl = s;
+        ev->c2 = (T)1 - s2;
+        ev->half_phi = (T)3.141592653589793 * uphi;
+        ev->x = x0;
+        ev->y = y0;
+        ev->z = z0;
+        ev->ch = MCD_CH_RUTH;
+    }
+    const bool left = L.outcome != MCD_OUT_NONE;
+    if (!left || (c.quirks & MCD_Q_CROSSING_STEP)) lane_lose(L, c, dE);
+    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
+    return MCD_CH_RUTH;
+}
+
+// ---------------------------------------------------------------------------
+// warp-aggregated append of one record per calling lane to the event ring
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void ring_append(const mcd_event_ring& ring, uint32_t electron, int64_t step,
+                                            const EventOut<T>& ev) {
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    const unsigned rank = __popc(mask & ((1u << lane) - 1u));
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(ring.cursor, (unsigned long long)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    const unsigned long long slot = base + rank;
+    if (slot < ring.capacity) {
+        mcd_event e;
+        e.electron = electron;
+        e.step_chan = ((uint32_t)(step - 1) << 5) | (uint32_t)(ev.ch & 31);
+        e.E = (float)ev.E;
+        e.W = (float)ev.W;
+        e.pathl = (float)ev.pathl;
+        e.c2 = (float)ev.c2;
+        e.half_phi = (float)ev.half_phi;
+        e.x = (float)ev.x;
+        e.y = (float)ev.y;
+        e.z = (float)ev.z;
+        ring.rec[slot] = e;
+    }
+}
+
+}  // namespace mcd
+
+#endif  // MCD_DEVICE_CUH

@@ -1,0 +1,401 @@
+// mcd_transport.cu - trajectory kernels and their C-ABI entry points.
+//
+//  k_plain    one thread per electron, one launch per simulation
+//             (replaces multiTraj_DS/_cont, MC/tools/multiScatter.py:66-229)
+//  k_batched  persistent grid over many simulations; a global queue hands
+//             out electrons and a warp takes new ones as soon as `refill` of
+//             its lanes are idle, so uneven trajectory lengths do not idle
+//             the warp (replaces MapScatterer's pool, MC/doScatter.py:22-95)
+//
+// Tallies are gathered per block in shared memory and flushed once per block
+// with global atomics; exit-energy/angle histograms go straight to global
+// memory (one atomic per backscattered electron).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "mcd_device.cuh"
+
+namespace mcd {
+
+struct BlockTally {
+    unsigned int outcome[8];
+    unsigned int double_rows, nan_events, clamped, long_path, table_range, pad_;
+    unsigned long long events;
+    double sum_E, sum_E2, sum_steps2;
+    unsigned int channel[MCD_MAX_CHANNELS];
+};
+
+__device__ __forceinline__ void bt_zero(BlockTally* t, int n) {
+    unsigned int* p = reinterpret_cast<unsigned int*>(t);
+    const int words = n * (int)(sizeof(BlockTally) / 4);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) p[i] = 0u;
+}
+
+__device__ __forceinline__ void add_u64(unsigned long long* p, unsigned long long v) {
+    if (v) atomicAdd(p, v);
+}
+
+__device__ __forceinline__ void bt_flush(const BlockTally& t, mcd_tally* g) {
+    // called by one thread per simulation
+    bool any = t.events != 0;
+    for (int k = 0; k < 8; ++k) any |= t.outcome[k] != 0;
+    if (!any) return;
+    for (int k = 0; k < 8; ++k) add_u64(&g->outcome[k], t.outcome[k]);
+    add_u64(&g->events, t.events);
+    add_u64(&g->double_rows, t.double_rows);
+    add_u64(&g->nan_events, t.nan_events);
+    add_u64(&g->clamped, t.clamped);
+    add_u64(&g->long_path, t.long_path);
+    add_u64(&g->table_range, t.table_range);
+    for (int k = 0; k < MCD_MAX_CHANNELS; ++k) add_u64(&g->channel[k], t.channel[k]);
+    if (t.sum_E != 0.0) atomicAdd(&g->sum_E_bks, t.sum_E);
+    if (t.sum_E2 != 0.0) atomicAdd(&g->sum_E2_bks, t.sum_E2);
+    if (t.sum_steps2 != 0.0) atomicAdd(&g->sum_steps2, t.sum_steps2);
+}
+
+struct ElOut {
+    uint8_t* outcome;
+    uint8_t* flags;
+    void* final_E;
+    void* dir;
+    void* last_pos;
+    void* max_z;
+    int32_t* n_events;
+};
+
+template <class T, class C>
+__device__ __forceinline__ uint32_t finish_electron(const C& c, const Lane<T>& L, uint64_t i, BlockTally& bt,
+                                                    mcd_tally* gt, const ElOut& eo) {
+    atomicAdd(&bt.outcome[L.outcome & 7], 1u);
+    atomicAdd(&bt.events, (unsigned long long)L.step);
+    atomicAdd(&bt.sum_steps2, (double)L.step * (double)L.step);
+    if (L.flags & F_DOUBLE_ROW) atomicAdd(&bt.double_rows, 1u);
+    if (L.nan_n) atomicAdd(&bt.nan_events, L.nan_n);
+    if (L.clamp_n) atomicAdd(&bt.clamped, L.clamp_n);
+    if (L.lpath_n) atomicAdd(&bt.long_path, L.lpath_n);
+    if (L.flags & F_TABLE_RANGE) atomicAdd(&bt.table_range, 1u);
+    if (L.outcome == MCD_OUT_BKS) {
+        const double e = (double)L.E_row;
+        atomicAdd(&bt.sum_E, e);
+        atomicAdd(&bt.sum_E2, e * e);
+        if (c.hE > 0) {
+            const T f = L.E_row * c.invWE;
+            if (f >= (T)0 && f < (T)c.hE) atomicAdd(&gt->hist_E[(int)f], 1ull);
+        }
+        if (c.hT > 0) {
+            const T th = Ops<T>::acos_deg(-L.dz) * c.invWT;
+            if (th >= (T)0 && th < (T)c.hT) atomicAdd(&gt->hist_T[(int)th], 1ull);
+        }
+    }
+    if (eo.outcome) eo.outcome[i] = (uint8_t)L.outcome;
+    if (eo.flags) eo.flags[i] = (uint8_t)(L.flags & (F_DOUBLE_ROW | F_NAN));
+    const size_t n = (size_t)c.num_el;
+    if (eo.final_E) static_cast<T*>(eo.final_E)[i] = L.E_row;
+    if (eo.dir) {
+        T* d = static_cast<T*>(eo.dir);
+        d[i] = L.dx;
+        d[n + i] = L.dy;
+        d[2 * n + i] = L.dz;
+    }
+    if (eo.last_pos) {
+        T* p = static_cast<T*>(eo.last_pos);
+        p[i] = L.x;
+        p[n + i] = L.y;
+        p[2 * n + i] = L.z;
+    }
+    if (eo.max_z) static_cast<T*>(eo.max_z)[i] = L.max_z;
+    if (eo.n_events) eo.n_events[i] = (int32_t)L.step;
+    uint32_t st = 0;
+    if (L.flags & F_NAN) st |= MCD_FLAG_NAN;
+    if (L.flags & F_TABLE_RANGE) st |= MCD_FLAG_TABLE_RANGE;
+    if (L.flags & F_CLAMPED) st |= MCD_FLAG_CLAMPED;
+    if (L.flags & F_LONG_PATH) st |= MCD_FLAG_LONG_PATH;
+    if (L.outcome == MCD_OUT_LONG) st |= MCD_FLAG_LONG;
+    return st;
+}
+
+__device__ __forceinline__ void or_status(uint32_t* status, uint32_t st) {
+    const uint32_t w = __reduce_or_sync(0xffffffffu, st);
+    if ((threadIdx.x & 31) == 0 && w) atomicOr(status, w);
+}
+
+// ---------------------------------------------------------------------------
+// plain kernel: one thread per electron
+// ---------------------------------------------------------------------------
+template <class T, int MODE, bool REC>
+__global__ void __launch_bounds__(256) k_plain(const SimConst<T> c, mcd_tally* tally, const ElOut eo,
+                                               const mcd_event_ring ring, uint32_t* status) {
+    __shared__ BlockTally bt;
+    bt_zero(&bt, 1);
+    __syncthreads();
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t st = 0;
+    if (i < (uint64_t)c.num_el) {
+        Lane<T> L;
+        lane_init(L, c);
+        const uint64_t elec = c.first + i;
+        const bool chan = (c.tally_flags & MCD_TALLY_CHANNELS) != 0;
+        while (L.outcome == MCD_OUT_NONE) {
+            EventOut<T> ev;
+            const int ch = (MODE == MCD_MODE_DS) ? ds_event<T, REC>(L, c, elec, &ev)
+                                                 : cont_event<T, REC>(L, c, elec, &ev);
+            if (ch >= 0) {
+                if (REC) ring_append(ring, (uint32_t)i, L.step, ev);
+                if (chan) atomicAdd(&bt.channel[ch], 1u);
+            }
+        }
+        st = finish_electron(c, L, i, bt, tally, eo);
+    }
+    or_status(status, st);
+    __syncthreads();
+    if (threadIdx.x == 0) bt_flush(bt, tally);
+}
+
+// ---------------------------------------------------------------------------
+// batched persistent kernel
+// ---------------------------------------------------------------------------
+struct BatchHeader {
+    unsigned long long queue;   // next electron to hand out
+    unsigned long long total;   // electrons over all simulations
+    int32_t nsims;
+    int32_t pad_[11];
+};
+
+constexpr int kBatchMaxSims = 256;
+
+__host__ __device__ inline size_t batch_prefix_off() { return sizeof(BatchHeader); }
+__host__ __device__ inline size_t batch_consts_off(int nsims) {
+    size_t o = sizeof(BatchHeader) + sizeof(unsigned long long) * (size_t)(nsims + 1);
+    return (o + 255) & ~(size_t)255;
+}
+__host__ __device__ inline size_t batch_bytes(int nsims) {
+    return batch_consts_off(nsims) + sizeof(SimConst<float>) * (size_t)nsims;
+}
+
+__host__ __device__ inline size_t batch_smem(int nsims) {
+    return sizeof(SimConst<float>) * nsims + sizeof(unsigned long long) * (nsims + 1) +
+           sizeof(BlockTally) * nsims;
+}
+
+template <int MODE_MIX>
+__global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallies, int refill,
+                                                  uint32_t* status) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    BatchHeader* hdr = reinterpret_cast<BatchHeader*>(ws);
+    const int nsims = hdr->nsims;
+    const unsigned long long total = hdr->total;
+    SimConst<float>* s_c = reinterpret_cast<SimConst<float>*>(smem);
+    unsigned long long* s_pre = reinterpret_cast<unsigned long long*>(smem + sizeof(SimConst<float>) * nsims);
+    BlockTally* s_t = reinterpret_cast<BlockTally*>(smem + sizeof(SimConst<float>) * nsims +
+                                                    sizeof(unsigned long long) * (nsims + 1));
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(ws + batch_consts_off(nsims));
+        uint32_t* dst = reinterpret_cast<uint32_t*>(s_c);
+        const int words = (int)(sizeof(SimConst<float>) / 4) * nsims;
+        for (int k = threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
+        const unsigned long long* pre = reinterpret_cast<const unsigned long long*>(ws + batch_prefix_off());
+        for (int k = threadIdx.x; k <= nsims; k += blockDim.x) s_pre[k] = pre[k];
+        bt_zero(s_t, nsims);
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    Lane<float> L;
+    int sim = 0;
+    uint64_t local = 0;
+    bool have = false;
+    bool exhausted = false;
+    uint32_t st = 0;
+    const ElOut eo{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !have);
+        if (!exhausted && idle && (__popc(idle) >= refill || idle == 0xffffffffu)) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&hdr->queue, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (!have) {
+                const unsigned long long g = base + __popc(idle & lt);
+                if (g < total) {
+                    int lo = 0, hi = nsims;  // s_pre[lo] <= g < s_pre[hi]
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_pre[mid] <= g) lo = mid; else hi = mid;
+                    }
+                    sim = lo;
+                    local = g - s_pre[lo];
+                    lane_init(L, s_c[sim]);
+                    have = true;
+                }
+            }
+            if (base + __popc(idle) >= total) exhausted = true;
+        }
+        if (!__any_sync(0xffffffffu, have)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (have) {
+            const SimConst<float>& c = s_c[sim];
+            EventOut<float> ev;
+            int ch;
+            if (MODE_MIX == 0 || c.mode == MCD_MODE_DS)
+                ch = ds_event<float, false>(L, c, c.first + local, &ev);
+            else
+                ch = cont_event<float, false>(L, c, c.first + local, &ev);
+            if (ch >= 0 && (c.tally_flags & MCD_TALLY_CHANNELS)) atomicAdd(&s_t[sim].channel[ch], 1u);
+            if (L.outcome != MCD_OUT_NONE) {
+                st |= finish_electron(c, L, local, s_t[sim], tallies + sim, eo);
+                have = false;
+            }
+        }
+    }
+    or_status(status, st);
+    __syncthreads();
+    for (int k = threadIdx.x; k < nsims; k += blockDim.x) bt_flush(s_t[k], tallies + k);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <class T, int MODE, bool REC>
+static int launch_plain(const SimConst<T>& c, int block, mcd_tally* tally, const ElOut& eo,
+                        const mcd_event_ring& ring, uint32_t* status, cudaStream_t st) {
+    const unsigned long long grid = ((unsigned long long)c.num_el + block - 1) / block;
+    if (grid == 0) return MCD_OK;
+    if (grid > 0x7fffffffull) return MCD_ETOOBIG;
+    k_plain<T, MODE, REC><<<(unsigned)grid, block, 0, st>>>(c, tally, eo, ring, status);
+    return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
+}
+
+template <class T>
+static int dispatch_plain(const SimConst<T>& c, int block, mcd_tally* tally, const ElOut& eo,
+                          const mcd_event_ring& ring, bool rec, uint32_t* status, cudaStream_t st) {
+    if (c.mode == MCD_MODE_DS)
+        return rec ? launch_plain<T, MCD_MODE_DS, true>(c, block, tally, eo, ring, status, st)
+                   : launch_plain<T, MCD_MODE_DS, false>(c, block, tally, eo, ring, status, st);
+    return rec ? launch_plain<T, MCD_MODE_CONT, true>(c, block, tally, eo, ring, status, st)
+               : launch_plain<T, MCD_MODE_CONT, false>(c, block, tally, eo, ring, status, st);
+}
+
+}  // namespace mcd
+
+using namespace mcd;
+
+extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_table* moller,
+                       const mcd_table* gryz, mcd_tally* tally, const mcd_electron_out* electrons,
+                       const mcd_event_ring* ring, uint32_t* status, int32_t block_size, void* stream) {
+    if (!sim || !mat || !tally || !status) return MCD_EINVAL;
+    const int rc = check_sim(*sim, *mat, moller, gryz);
+    if (rc != MCD_OK) return rc;
+    if (block_size <= 0) block_size = 128;
+    if (block_size % 32 != 0 || block_size > 256) return MCD_EINVAL;
+    ElOut eo{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (electrons) {
+        eo.outcome = electrons->outcome;
+        eo.flags = electrons->flags;
+        eo.final_E = electrons->final_E;
+        eo.dir = electrons->dir;
+        eo.last_pos = electrons->last_pos;
+        eo.max_z = electrons->max_z;
+        eo.n_events = electrons->n_events;
+    }
+    mcd_event_ring rg{nullptr, 0, nullptr};
+    bool rec = false;
+    if (ring && ring->rec && ring->cursor && ring->capacity > 0) {
+        rg = *ring;
+        rec = true;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const mcd_table* tm = sim->mode == MCD_MODE_DS ? moller : nullptr;
+    const mcd_table* tg = sim->mode == MCD_MODE_DS ? gryz : nullptr;
+    if (sim->precision == MCD_FP64)
+        return dispatch_plain<double>(make_consts<double>(*sim, *mat, tm, tg), block_size, tally, eo, rg, rec,
+                                      status, st);
+    return dispatch_plain<float>(make_consts<float>(*sim, *mat, tm, tg), block_size, tally, eo, rg, rec, status,
+                                 st);
+}
+
+extern "C" size_t mcd_batch_workspace_bytes(int32_t nsims) {
+    if (nsims <= 0 || nsims > kBatchMaxSims) return 0;
+    return batch_bytes(nsims);
+}
+
+extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_material* mats,
+                                 const int32_t* sim_material, const mcd_table* tables, const int32_t* sim_moller,
+                                 const int32_t* sim_gryz, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!sims || !mats || !sim_material || !workspace) return MCD_EINVAL;
+    if (nsims <= 0) return MCD_EINVAL;
+    if (nsims > kBatchMaxSims) return MCD_ETOOBIG;
+    if (workspace_bytes < batch_bytes(nsims)) return MCD_EINVAL;
+    if ((reinterpret_cast<uintptr_t>(workspace) & 255) != 0) return MCD_EINVAL;
+    const size_t bytes = batch_bytes(nsims);
+    uint8_t* host = static_cast<uint8_t*>(calloc(1, bytes));
+    if (!host) return MCD_EINVAL;
+    BatchHeader* h = reinterpret_cast<BatchHeader*>(host);
+    unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + batch_prefix_off());
+    SimConst<float>* cs = reinterpret_cast<SimConst<float>*>(host + batch_consts_off(nsims));
+    unsigned long long acc = 0;
+    int rc = MCD_OK;
+    for (int k = 0; k < nsims && rc == MCD_OK; ++k) {
+        const mcd_sim& s = sims[k];
+        const mcd_material& m = mats[sim_material[k]];
+        const mcd_table* tm = nullptr;
+        const mcd_table* tg = nullptr;
+        if (s.mode == MCD_MODE_DS) {
+            if (!tables || !sim_moller || !sim_gryz) { rc = MCD_EINVAL; break; }
+            tm = &tables[sim_moller[k]];
+            tg = &tables[sim_gryz[k]];
+        }
+        rc = check_sim(s, m, tm, tg);
+        if (rc != MCD_OK) break;
+        if (s.precision != MCD_FP32) { rc = MCD_EINVAL; break; }
+        pre[k] = acc;
+        acc += (unsigned long long)s.num_el;
+        cs[k] = make_consts<float>(s, m, tm, tg);
+    }
+    pre[nsims] = acc;
+    h->queue = 0;
+    h->total = acc;
+    h->nsims = nsims;
+    if (rc == MCD_OK) {
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (cudaMemcpyAsync(workspace, host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = MCD_ECUDA;
+        else if (cudaStreamSynchronize(st) != cudaSuccess) rc = MCD_ECUDA;
+    }
+    free(host);
+    return rc;
+}
+
+extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallies, const mcd_tune* tune,
+                               uint32_t* status, void* stream) {
+    if (!workspace || !tallies || !status) return MCD_EINVAL;
+    if (nsims <= 0) return MCD_EINVAL;
+    if (nsims > kBatchMaxSims) return MCD_ETOOBIG;
+    int block = 256, per_sm = 0, refill = 1;
+    if (tune) {
+        if (tune->block_size > 0) block = tune->block_size;
+        if (tune->blocks_per_sm > 0) per_sm = tune->blocks_per_sm;
+        if (tune->refill > 0) refill = tune->refill;
+    }
+    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
+    const size_t smem = batch_smem(nsims);
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(k_batched<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return MCD_ECUDA;
+    }
+    int fit = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<1>, block, smem) != cudaSuccess)
+        return MCD_ECUDA;
+    if (fit < 1) return MCD_ETOOBIG;
+    if (per_sm <= 0 || per_sm > fit) per_sm = fit;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // reset the queue (the first word of the workspace)
+    if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
+    k_batched<1><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status);
+    return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
+}

@@ -1,0 +1,294 @@
+"""Host engine: builds mcd_sim structs from input.file parameters, owns the
+device buffers (torch tensors) and calls the C ABI on the current stream.
+
+    run(input_par, num_el, seed)          one simulation, one launch
+    Batch(sims).run(tune)                 many simulations, one persistent launch
+
+Everything is device-resident; results are copied back only when asked.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from .config import with_defaults
+from .tables import ds_tables
+
+DEFAULT_HIST_E = (200, 100.0)   # 200 bins of 100 eV
+DEFAULT_HIST_T = (90, 1.0)      # 90 bins of 1 degree
+
+_DTYPE = {_lib.FP32: np.float32, _lib.FP64: np.float64}
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("mcd needs a CUDA device (there is no CPU path)")
+    return torch
+
+
+def mode_of(input_par):
+    return _lib.MODE_DS if "DS" in input_par.get("mode", "DS") else _lib.MODE_CONT
+
+
+def make_sim(input_par, num_el, seed=0, first_electron=0, precision=_lib.FP32, sim_id=0,
+             hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
+             tally_flags=0, J_scale=1.0, n_scale=1.0):
+    p = with_defaults(input_par)
+    s = _lib.Sim()
+    s.mode = mode_of(p)
+    s.bethe_model = _lib.BETHE[p.get("Bethe_model", "classical")]
+    s.precision = precision
+    s.quirks = quirks
+    s.tally_flags = tally_flags
+    s.sim_id = sim_id
+    s.E0 = float(p["E0"])
+    s.Emin = float(p["Emin"])
+    s.s_tilt = float(p["s_tilt"])
+    s.Wc = float(p["Wc"])
+    s.thickness = float(p["thickness"])
+    s.max_scatt = int(p["maxScatt"])
+    s.num_el = int(num_el)
+    s.first_electron = int(first_electron)
+    s.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    s.hist_E_bins, s.hist_E_width = int(hist_E[0]), float(hist_E[1])
+    s.hist_T_bins, s.hist_T_width = int(hist_T[0]), float(hist_T[1])
+    s.J_scale = float(J_scale)
+    s.n_scale = float(n_scale)
+    if p.get("elastic", "Ruth_vanilla") != "Ruth_vanilla":
+        raise NotImplementedError("elastic model %r: only Ruth_vanilla is on the GPU path" % p["elastic"])
+    if p.get("diffMFP"):
+        raise NotImplementedError("diffMFP: the diffraction channel is not on the GPU path")
+    return s
+
+
+def tally_to_dict(t):
+    out = {k: int(t.outcome[i]) for i, k in enumerate(_lib.OUTCOME_NAMES)}
+    for k in ("events", "double_rows", "nan_events", "clamped", "long_path", "table_range"):
+        out[k] = int(getattr(t, k))
+    out["channel"] = np.array(t.channel[:], dtype=np.int64)
+    out["sum_E_bks"] = float(t.sum_E_bks)
+    out["sum_E2_bks"] = float(t.sum_E2_bks)
+    out["sum_steps2"] = float(t.sum_steps2)
+    out["hist_E"] = np.array(t.hist_E[:], dtype=np.int64)
+    out["hist_T"] = np.array(t.hist_T[:], dtype=np.int64)
+    return out
+
+
+def tally_from_bytes(buf):
+    t = _lib.Tally.from_buffer_copy(bytes(buf))
+    return tally_to_dict(t)
+
+
+class RunBuffers:
+    """Device buffers of one simulation (re-usable across launches)."""
+
+    def __init__(self, num_el, precision=_lib.FP32, electrons=True, ring_capacity=0, device="cuda"):
+        torch = _torch()
+        self.device = torch.device(device)
+        self.num_el = int(num_el)
+        self.precision = precision
+        tsz = C.sizeof(_lib.Tally)
+        self.tally = torch.zeros(tsz, dtype=torch.uint8, device=self.device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        fdt = torch.float32 if precision == _lib.FP32 else torch.float64
+        self.el = None
+        if electrons:
+            n = self.num_el
+            self.el = dict(
+                outcome=torch.zeros(n, dtype=torch.uint8, device=self.device),
+                flags=torch.zeros(n, dtype=torch.uint8, device=self.device),
+                final_E=torch.zeros(n, dtype=fdt, device=self.device),
+                dir=torch.zeros(3 * n, dtype=fdt, device=self.device),
+                last_pos=torch.zeros(3 * n, dtype=fdt, device=self.device),
+                max_z=torch.zeros(n, dtype=fdt, device=self.device),
+                n_events=torch.zeros(n, dtype=torch.int32, device=self.device),
+            )
+        self.ring = None
+        if ring_capacity:
+            self.ring = torch.zeros((int(ring_capacity), C.sizeof(_lib.Event)), dtype=torch.uint8,
+                                    device=self.device)
+            self.cursor = torch.zeros(1, dtype=torch.int64, device=self.device)
+
+    def zero(self):
+        self.tally.zero_()
+        self.status.zero_()
+        if self.ring is not None:
+            self.cursor.zero_()
+
+    def electron_struct(self):
+        if self.el is None:
+            return None
+        e = self.el
+        return _lib.ElectronOut(e["outcome"].data_ptr(), e["flags"].data_ptr(), e["final_E"].data_ptr(),
+                                e["dir"].data_ptr(), e["last_pos"].data_ptr(), e["max_z"].data_ptr(),
+                                e["n_events"].data_ptr())
+
+    def ring_struct(self):
+        if self.ring is None:
+            return None
+        return _lib.EventRing(self.ring.data_ptr(), self.ring.shape[0], self.cursor.data_ptr())
+
+
+class RunResult:
+    def __init__(self, tally, status, electrons=None, events=None, events_total=0):
+        self.tally = tally
+        self.status = status
+        self.electrons = electrons
+        self.events = events
+        self.events_total = events_total
+
+    @property
+    def eta(self):
+        n = sum(self.tally[k] for k in _lib.OUTCOME_NAMES)
+        return self.tally["bks"] / n if n else float("nan")
+
+
+EVENT_DTYPE = np.dtype([("electron", "<u4"), ("step_chan", "<u4"), ("E", "<f4"), ("W", "<f4"),
+                        ("pathl", "<f4"), ("c2", "<f4"), ("half_phi", "<f4"), ("x", "<f4"),
+                        ("y", "<f4"), ("z", "<f4")])
+
+
+def launch(sim, mat, tables, bufs, block_size=128, stream=None):
+    """Enqueue one mcd_run on `stream` (torch's current stream by default)."""
+    torch = _torch()
+    st = stream if stream is not None else torch.cuda.current_stream(bufs.device)
+    tm = tables[0].struct if tables else None
+    tg = tables[1].struct if tables else None
+    el = bufs.electron_struct()
+    rg = bufs.ring_struct()
+    code = _lib.lib().mcd_run(C.byref(sim), C.byref(mat), C.byref(tm) if tm else None,
+                              C.byref(tg) if tg else None, bufs.tally.data_ptr(),
+                              C.byref(el) if el else None, C.byref(rg) if rg else None,
+                              bufs.status.data_ptr(), int(block_size), st.cuda_stream)
+    _lib.check("mcd_run", code)
+
+
+def collect(bufs):
+    """Copy the results of the last launch back to the host (synchronises)."""
+    tally = tally_from_bytes(bufs.tally.cpu().numpy())
+    status = int(bufs.status.item())
+    electrons = None
+    if bufs.el is not None:
+        n = bufs.num_el
+        e = {k: v.cpu().numpy() for k, v in bufs.el.items()}
+        electrons = dict(outcome=e["outcome"], flags=e["flags"], final_E=e["final_E"],
+                         dir=e["dir"].reshape(3, n).T.copy(), last_pos=e["last_pos"].reshape(3, n).T.copy(),
+                         max_z=e["max_z"], n_events=e["n_events"])
+    events, total = None, 0
+    if bufs.ring is not None:
+        total = int(bufs.cursor.item())
+        k = min(total, bufs.ring.shape[0])
+        events = bufs.ring[:k].cpu().numpy().view(EVENT_DTYPE).reshape(-1)
+        if total > bufs.ring.shape[0]:
+            status |= _lib.FLAG_RING_FULL
+    return RunResult(tally, status, electrons, events, total)
+
+
+def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", electrons=True, ring_capacity=0,
+        tally_channels=False, hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
+        J_scale=1.0, n_scale=1.0, block_size=128, device="cuda", tables=None):
+    """Run one simulation to completion and return its results on the host."""
+    _torch()
+    p = with_defaults(input_par)
+    n = int(p["num_el"] if num_el is None else num_el)
+    prec = _lib.FP64 if precision in ("fp64", _lib.FP64) else _lib.FP32
+    mat = _lib.material(p["material"])
+    sim = make_sim(p, n, seed, first_electron, prec, 0, hist_E, hist_T, quirks,
+                   _lib.TALLY_CHANNELS if tally_channels else 0, J_scale, n_scale)
+    if sim.mode == _lib.MODE_DS and tables is None:
+        tables = ds_tables(mat, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"], device)
+    bufs = RunBuffers(n, prec, electrons, ring_capacity, device)
+    bufs.zero()
+    launch(sim, mat, tables if sim.mode == _lib.MODE_DS else None, bufs, block_size)
+    return collect(bufs)
+
+
+# ---------------------------------------------------------------------------
+# batched persistent launch
+# ---------------------------------------------------------------------------
+class Batch:
+    """Many simulations run by one persistent kernel.
+
+    sims: list of input_par dicts (each with num_el).  Tables are built once
+    per distinct (material, E0, Emin, Wc, tol) and shared.
+    """
+
+    def __init__(self, sims, seed=0, device="cuda", hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T,
+                 quirks=_lib.QUIRKS_REFERENCE, tally_channels=False, first_electron=0):
+        torch = _torch()
+        self.device = torch.device(device)
+        self.inputs = [with_defaults(s) for s in sims]
+        self.n = len(self.inputs)
+        mats, mat_index = [], {}
+        tabs, tab_index = [], {}
+        sim_mat, sim_m, sim_g = [], [], []
+        self.structs = []
+        for k, p in enumerate(self.inputs):
+            sp = p["material"]
+            if sp not in mat_index:
+                mat_index[sp] = len(mats)
+                mats.append(_lib.material(sp))
+            mi = mat_index[sp]
+            sim_mat.append(mi)
+            if mode_of(p) == _lib.MODE_DS:
+                key = (sp, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"])
+                if key not in tab_index:
+                    tm, tg = ds_tables(mats[mi], *key[1:], device=device)
+                    tab_index[key] = len(tabs)
+                    tabs += [tm, tg]
+                sim_m.append(tab_index[key])
+                sim_g.append(tab_index[key] + 1)
+            else:
+                sim_m.append(0)
+                sim_g.append(0)
+            self.structs.append(make_sim(p, p["num_el"], seed, first_electron, _lib.FP32, k, hist_E, hist_T, quirks,
+                                         _lib.TALLY_CHANNELS if tally_channels else 0))
+        self.tables = tabs
+        self.mats = (_lib.Material * len(mats))(*mats)
+        self._sims_arr = (_lib.Sim * self.n)(*self.structs)
+        self._tarr = (_lib.Table * max(1, len(tabs)))(*[t.struct for t in tabs]) if tabs else None
+        ia = lambda v: (C.c_int32 * self.n)(*v)  # noqa: E731
+        self._idx = (ia(sim_mat), ia(sim_m), ia(sim_g))
+        nbytes = _lib.lib().mcd_batch_workspace_bytes(self.n)
+        if nbytes == 0:
+            raise _lib.MCDError("mcd_batch_workspace_bytes", _lib.ETOOBIG)
+        self.workspace = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
+        off = (-self.workspace.data_ptr()) % 256
+        self.ws_ptr = self.workspace.data_ptr() + off
+        self.ws_bytes = nbytes
+        self.prepare()
+        self.tallies = torch.zeros((self.n, C.sizeof(_lib.Tally)), dtype=torch.uint8, device=self.device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.total_electrons = sum(int(p["num_el"]) for p in self.inputs)
+
+    def prepare(self, stream=None):
+        """Pack the simulations into the device workspace (host-to-device copy)."""
+        torch = _torch()
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        code = _lib.lib().mcd_batch_prepare(self._sims_arr, self.n, self.mats, self._idx[0], self._tarr,
+                                            self._idx[1], self._idx[2], self.ws_ptr, self.ws_bytes,
+                                            st.cuda_stream)
+        _lib.check("mcd_batch_prepare", code)
+
+    def launch(self, tune=None, stream=None):
+        torch = _torch()
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        t = tune if tune is not None else _lib.Tune(256, 0, 1, 0, 0)
+        code = _lib.lib().mcd_run_batched(self.ws_ptr, self.n, self.tallies.data_ptr(), C.byref(t),
+                                          self.status.data_ptr(), st.cuda_stream)
+        _lib.check("mcd_run_batched", code)
+
+    def zero(self):
+        self.tallies.zero_()
+        self.status.zero_()
+
+    def run(self, tune=None):
+        self.zero()
+        self.launch(tune)
+        return self.collect()
+
+    def collect(self):
+        host = self.tallies.cpu().numpy()
+        return [tally_from_bytes(host[k]) for k in range(self.n)], int(self.status.item())

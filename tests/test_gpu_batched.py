@@ -1,0 +1,74 @@
+"""The batched persistent kernel against one plain launch per simulation.
+
+Both run the same event code on the same Philox counters (sim id, electron,
+event), so the integer tallies must agree; the refill setting only changes
+which lane runs which electron, never the result."""
+import numpy as np
+import pytest
+
+from mcd import _lib, engine
+from _gpu_util import eta_z, input_par
+
+pytestmark = pytest.mark.gpu
+
+SIMS = [
+    dict(input_par("Si", 10000.0, 1000.0, 0.0), num_el=3000),
+    dict(input_par("Au", 20000.0, 1000.0, 45.0), num_el=700),
+    dict(input_par("Cu", 5000.0, 1000.0, 70.0), num_el=5000),
+    dict(input_par("Al", 30000.0, 1000.0, 20.0), num_el=1200),
+    dict(input_par("Cu", 20000.0, 1000.0, 70.0, mode="cont", bethe="JL"), num_el=2500),
+    dict(input_par("Al", 15000.0, 1000.0, 70.0, mode="cont", bethe="classical"), num_el=64),
+]
+
+INT_KEYS = ("none", "bks", "abs", "trsm", "trdf", "long", "events", "double_rows", "nan_events",
+            "clamped", "long_path", "table_range")
+
+
+def plain(k, p):
+    # the batched kernel uses sim id = index in the batch; match it here
+    mat = _lib.material(p["material"])
+    sim = engine.make_sim(p, p["num_el"], seed=42, sim_id=k)
+    tabs = None
+    if engine.mode_of(p) == _lib.MODE_DS:
+        from mcd.tables import ds_tables
+        tabs = ds_tables(mat, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"])
+    bufs = engine.RunBuffers(p["num_el"], _lib.FP32, False, 0)
+    bufs.zero()
+    engine.launch(sim, mat, tabs, bufs)
+    return engine.collect(bufs).tally
+
+
+@pytest.fixture(scope="module")
+def plain_tallies():
+    return [plain(k, p) for k, p in enumerate(SIMS)]
+
+
+@pytest.mark.parametrize("refill", [1, 8, 32])
+@pytest.mark.parametrize("block", [128, 256])
+def test_batched_equals_plain(plain_tallies, refill, block):
+    b = engine.Batch(SIMS, seed=42)
+    res, status = b.run(_lib.Tune(block, 0, refill, 0, 0))
+    for k, (t, ref) in enumerate(zip(res, plain_tallies)):
+        for key in INT_KEYS:
+            assert t[key] == ref[key], (k, key, t[key], ref[key])
+        assert np.array_equal(t["hist_E"], ref["hist_E"])
+        assert np.array_equal(t["hist_T"], ref["hist_T"])
+        assert abs(t["sum_E_bks"] - ref["sum_E_bks"]) <= 1e-9 * max(1.0, ref["sum_E_bks"])
+        assert sum(t[o] for o in ("bks", "abs", "trsm", "long")) == SIMS[k]["num_el"]
+
+
+def test_batched_relaunch_is_identical():
+    b = engine.Batch(SIMS[:4], seed=3)
+    r1, _ = b.run()
+    r2, _ = b.run()
+    for t1, t2 in zip(r1, r2):
+        for key in INT_KEYS:
+            assert t1[key] == t2[key]
+
+
+def test_batched_rejects_bad_tuning():
+    b = engine.Batch(SIMS[:1], seed=3)
+    with pytest.raises(_lib.MCDError):
+        b.launch(_lib.Tune(100, 0, 1, 0, 0))
+    with pytest.raises(_lib.MCDError):
+        b.launch(_lib.Tune(128, 0, 40, 0, 0))

@@ -1,0 +1,67 @@
+"""CUDA transport against the oracle on the same inputs.
+
+FP64 transport and the C oracle consume the same Philox stream and the same
+tables, so they follow the same trajectories: outcome, event count and exit
+energy agree electron by electron (a trajectory can still part where CUDA's
+log/sin and glibc's differ in the last bit right at a decision boundary,
+hence the 99% floor).  FP32 transport is checked against the oracle
+statistically and by its per-electron agreement rate.
+"""
+import numpy as np
+import pytest
+from scipy import stats
+
+from _gpu_util import eta_z, input_par, run_pair
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # name, input parameters, electrons
+    ("si10_ds", input_par("Si", 10000.0, 1000.0, 0.0), 3000),
+    ("cu20t45_ds", input_par("Cu", 20000.0, 1000.0, 45.0), 600),
+    ("au30t70_ds", input_par("Au", 30000.0, 500.0, 70.0, Wc=50.0, tol=1e-4), 200),
+    ("al15_cont_cl", input_par("Al", 15000.0, 1000.0, 70.0, mode="cont", bethe="classical"), 3000),
+    ("cu20_cont_jl", input_par("Cu", 20000.0, 1000.0, 70.0, mode="cont", bethe="JL"), 2000),
+    ("si10_cont_ex", input_par("Si", 10000.0, 1000.0, 0.0, mode="cont", bethe="explicit"), 2000),
+]
+
+
+@pytest.mark.parametrize("name,p,n", CASES, ids=[c[0] for c in CASES])
+def test_fp64_follows_oracle_trajectories(name, p, n):
+    g, c = run_pair(p, n, seed=123, precision="fp64")
+    e = g.electrons
+    same = (e["outcome"] == c["outcome"]) & (e["n_events"] == c["n_events"])
+    assert same.mean() >= 0.99, (name, same.mean())
+    fe_ok = np.abs(e["final_E"] - c["final_E"]) <= 1e-9 * np.abs(c["final_E"])
+    assert (same & fe_ok).mean() >= 0.99, name
+    d_ok = np.abs(e["dir"] - c["dir"]).max(axis=1) <= 1e-9
+    d_ok |= np.isnan(c["dir"]).any(axis=1) & np.isnan(e["dir"]).any(axis=1)
+    assert (same & d_ok).mean() >= 0.99, name
+    p_ok = np.abs(e["last_pos"] - c["last_pos"]).max(axis=1) <= 1e-9 * np.maximum(1.0, np.abs(c["last_pos"]).max(axis=1))
+    assert (same & p_ok).mean() >= 0.98, name
+    # tallies agree with the per-electron rows
+    t = g.tally
+    assert t["bks"] == int((e["outcome"] == 1).sum())
+    assert t["events"] == int(e["n_events"].sum())
+    assert t["bks"] + t["abs"] + t["trsm"] + t["long"] == n
+
+
+@pytest.mark.parametrize("name,p,n", CASES, ids=[c[0] for c in CASES])
+def test_fp32_matches_oracle_statistics(name, p, n):
+    n = n * 4
+    g, c = run_pair(p, n, seed=7, precision="fp32")
+    e = g.electrons
+    agree = np.mean((e["outcome"] == c["outcome"]) & (e["n_events"] == c["n_events"]))
+    assert agree > 0.5, agree      # same stream: most trajectories stay identical in FP32
+    k1 = int((e["outcome"] == 1).sum())
+    k2 = int((c["outcome"] == 1).sum())
+    assert eta_z(n, k1, n, k2) < 3.0
+    b1 = e["final_E"][e["outcome"] == 1]
+    b2 = c["final_E"][c["outcome"] == 1]
+    if min(b1.size, b2.size) > 20:
+        assert stats.ks_2samp(b1, b2).pvalue > 0.01
+    assert stats.ks_2samp(e["n_events"], c["n_events"]).pvalue > 0.01
+    # FP32 error against the FP64 oracle on the electrons that stayed identical
+    same = (e["outcome"] == c["outcome"]) & (e["n_events"] == c["n_events"])
+    relE = np.abs(e["final_E"][same] - c["final_E"][same]) / c["final_E"][same]
+    assert np.median(relE) < 1e-5

@@ -1,0 +1,141 @@
+"""Host logic and the C ABI, without a GPU: the library builds, loads and
+exports every function include/mcd.h declares; struct layouts agree; the
+host-only entry points (material constants) and the host grid search match
+the reference's golden values; the input.file parser keeps its semantics."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from mcd import _lib, config, tables
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "mcd.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mcd_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    names = declared_functions()
+    assert "mcd_run" in names and "mcd_build_table" in names
+    for name in names:
+        assert hasattr(L, name), name
+        assert name in _lib.SIGNATURES, "no ctypes signature for " + name
+
+
+def test_struct_layouts_match():
+    L = _lib.lib()
+    for name, cls in _lib.STRUCTS.items():
+        assert L.mcd_struct_size(name.encode()) == C.sizeof(cls), name
+    assert C.sizeof(_lib.Event) == 40
+
+
+def test_abi_and_errors():
+    L = _lib.lib()
+    assert L.mcd_abi_version() == 1
+    assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
+    m = _lib.Material()
+    assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
+    assert L.mcd_material_init(None, C.byref(m)) == _lib.EINVAL
+
+
+def test_entry_points_reject_bad_arguments_without_touching_the_gpu():
+    L = _lib.lib()
+    assert L.mcd_run(None, None, None, None, None, None, None, None, 128, None) == _lib.EINVAL
+    assert L.mcd_batch_workspace_bytes(0) == 0
+    assert L.mcd_batch_workspace_bytes(257) == 0
+    assert L.mcd_build_table(0, None, 0, 1, 2, None, None, None, None, None, None) == _lib.EINVAL
+    assert L.mcd_run_batched(None, 1, None, None, None, None) == _lib.EINVAL
+
+
+@pytest.mark.parametrize("sp", ["Al", "Si", "Cu", "Au"])
+def test_material_constants(golden, sp):
+    m = _lib.material(sp)
+    ref = golden["physics"][sp + "/const"]
+    got = np.array([m.atnd, m.plasmon_e, m.fermi_e])
+    assert np.max(np.abs(got - ref) / ref) < 1e-14
+    assert m.species.decode() == sp
+    assert m.n_shells == {"Al": 3, "Si": 3, "Cu": 4, "Au": 8}[sp]
+
+
+def test_grid_search_matches_reference(golden):
+    """The host grid search picks the reference's exact float32 W and E grids
+    for every table of the benchmark configurations."""
+    T = golden["tables"]
+    for key in T["names"]:
+        sp = str(T[key + "/species"])
+        kind = key.split("/")[1]
+        E0, Emin, Wc, tol = T[key + "/spec"]
+        Ws, Es = tables.find_grids(kind, _lib.material(sp), E0, Emin, Wc, tol, tol)
+        assert np.array_equal(Ws, T[key + "/Ws"]), key
+        assert np.array_equal(Es, T[key + "/Es"]), key
+
+
+def test_grid_search_fails_like_reference_for_deep_shells():
+    """Si 1s at tol 1e-3 has no grid within 1e6 points (the reference raises
+    StopIteration); the library raises TableBuildError."""
+    m = _lib.material("Si")
+
+    class Inner:
+        pass
+
+    spec = tables._Spec("Gryz", m, 10000.0, 1000.0, 100.0, 1e-3, 1e-3)
+    spec.Wmin = spec.Eb = 1189.0
+    spec.nfree = 2.0
+    spec.Emin = 1189.0
+    with pytest.raises(tables.TableBuildError):
+        Ws = tables.find_W_series(spec)
+        tables.find_E_series(spec, Ws)
+
+
+INPUT = """# a test input file
+num_el   : 64 #multiples of 4
+E0       : 15000 # eV
+Emin     : 1000
+material : Al
+s_tilt   : 70
+thickness :  5e5
+elastic  : Ruth_vanilla
+mode     : cont
+Bethe_model : JL
+diffMFP    : no
+gen_tables : yes
+tol_E : 1e-3
+tol_W : 1e-3
+maxScatt: 100000
+Wc       : 100
+electron_output : outcome, final_E, final_dir
+scatter_output : type, E_loss,pathl
+"""
+
+
+def test_input_parser(tmp_path):
+    f = tmp_path / "input.file"
+    f.write_text(INPUT)
+    p = config.readInput(str(f))
+    assert p["num_el"] == 64 and isinstance(p["num_el"], int)
+    assert p["E0"] == 15000.0 and isinstance(p["E0"], float)
+    assert p["material"] == "Al" and p["mode"] == "cont" and p["Bethe_model"] == "JL"
+    assert p["diffMFP"] is False and p["gen_tables"] is True
+    assert p["electron_output"] == ["outcome", "final_E", "final_dir"]
+    assert p["scatter_output"] == ["type", "E_loss", "pathl"]
+    assert p["thickness"] == 5e5 and p["maxScatt"] == 100000
+    q = config.with_defaults({"E0": 1.0})
+    assert q["E0"] == 1.0 and q["thickness"] == 1e30
+
+
+def test_sim_struct_from_input():
+    from mcd import engine
+    p = config.parse_input(INPUT)
+    s = engine.make_sim(p, 64, seed=3)
+    assert s.mode == _lib.MODE_CONT and s.bethe_model == _lib.BETHE["JL"]
+    assert s.num_el == 64 and s.seed == 3 and s.s_tilt == 70.0
+    with pytest.raises(NotImplementedError):
+        engine.make_sim(dict(p, elastic="Mott"), 1)
