@@ -44,13 +44,15 @@ MUFU_PER_EVENT = {k: 17 + 4 * n for k, n in N_SHELLS.items()}     # Si 29, Au 49
 CPU_SAMPLE_PER_SIM = 600
 
 
-def workload():
+def workload(scale=1.0):
     rng = np.random.default_rng(0)
     sims = []
     for m in MATERIALS:
         for E0 in ENERGIES:
             for t in TILTS:
                 n = int(round(10 ** rng.uniform(3, 6)))
+                if scale != 1.0:
+                    n = max(32, int(round(n * scale)))
                 sims.append(dict(material=m, E0=E0, Emin=1000.0, s_tilt=t, Wc=100.0, tol_E=1e-3, tol_W=1e-3,
                                  mode="DS", num_el=n))
     return sims
@@ -201,7 +203,7 @@ def run_mcd(args):
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
-    sims = workload()
+    sims = workload(args.scale)
     first = rank << 40            # disjoint Philox electron indices per rank
     tune = _lib.Tune(args.block, args.blocks_per_sm, args.refill, 0, 0)
 
@@ -247,7 +249,8 @@ def run_mcd(args):
 
     for _ in range(args.warmup):
         batched_step()
-        plain_step()
+        if not args.no_plain:
+            plain_step()
     torch.cuda.synchronize(dev)
     tallies, status = batch.collect()
     events = sum(t["events"] for t in tallies)
@@ -259,9 +262,12 @@ def run_mcd(args):
     t_batched = timed(batched_step, args.steps)
     barrier()
     clk = clocks.stop()
-    t_plain = timed(plain_step, max(1, args.steps // 2))
     k_plain = max(1, args.steps // 2)
-    ptallies = [engine.collect(b[3]).tally for b in plain]
+    if args.no_plain:
+        t_plain, ptallies = float("nan"), tallies
+    else:
+        t_plain = timed(plain_step, k_plain)
+        ptallies = [engine.collect(b[3]).tally for b in plain]
     barrier()
 
     # end to end through the public API: host-side inputs packed and copied
@@ -326,7 +332,10 @@ def run_mcd(args):
     ach = flop / kt / 1e12
     ach_mufu = mufu / kt / 1e12
 
-    cpu = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=1, seed=args.seed)
+    if args.no_cpu:
+        cpu = {"events": 0, "times": [float("nan")], "threads": 0}
+    else:
+        cpu = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=1, seed=args.seed)
     cpu_v = cpu["events"] / cpu["times"][0]
 
     line = {
@@ -369,6 +378,10 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--plain-block", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="multiply every num_el (profiling of small cases); 1 = the benchmark workload")
+    ap.add_argument("--no-plain", action="store_true", help="skip the 64-launch plain path")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

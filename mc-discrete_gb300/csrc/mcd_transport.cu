@@ -123,10 +123,17 @@ __device__ __forceinline__ void or_status(uint32_t* status, uint32_t st) {
 // ---------------------------------------------------------------------------
 // plain kernel: one thread per electron
 // ---------------------------------------------------------------------------
+// The constant block arrives as a by-value kernel parameter and is copied to
+// shared memory before use.  Reading it through a reference to the parameter
+// itself made nvcc 13.0 (sm_103a, -O3) drop the loop-carried energy update of
+// the lane state initialised from it; the shared-memory copy is also what the
+// batched kernel reads.
 template <class T, int MODE, bool REC>
-__global__ void __launch_bounds__(256) k_plain(const SimConst<T> c, mcd_tally* tally, const ElOut eo,
+__global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* tally, const ElOut eo,
                                                const mcd_event_ring ring, uint32_t* status) {
     __shared__ BlockTally bt;
+    __shared__ SimConst<T> c;
+    if (threadIdx.x == 0) c = cp;
     bt_zero(&bt, 1);
     __syncthreads();
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

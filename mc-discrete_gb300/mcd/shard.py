@@ -1,0 +1,57 @@
+"""Splitting electrons across GPUs (one process per GPU).
+
+Every electron owns its Philox counter range (event, electron index, sim), so
+a simulation split into contiguous index ranges gives exactly the electrons a
+single process would: there is no data exchange while transporting, and the
+only exchange is one sum of the integer/FP64 tallies at the end.
+"""
+import numpy as np
+
+INT_KEYS = ("none", "bks", "abs", "trsm", "trdf", "long", "events", "double_rows", "nan_events",
+            "clamped", "long_path", "table_range")
+SUM_KEYS = ("sum_E_bks", "sum_E2_bks", "sum_steps2")
+ARRAY_KEYS = ("channel", "hist_E", "hist_T")
+
+
+def shard_range(num_el, world, rank, first=0):
+    """(first electron index, count) of `rank`'s contiguous share."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad world/rank")
+    lo = num_el * rank // world
+    hi = num_el * (rank + 1) // world
+    return first + lo, hi - lo
+
+
+def replica_offset(rank, bits=40):
+    """First electron index of a replica that runs the whole workload on its
+    own indices (weak scaling): 2^40 electrons apart."""
+    return int(rank) << bits
+
+
+def merge_tallies(tallies):
+    """Sum per-shard tally dicts (as returned by mcd.engine) into one."""
+    out = {}
+    for k in INT_KEYS:
+        out[k] = int(sum(t[k] for t in tallies))
+    for k in SUM_KEYS:
+        out[k] = float(sum(t[k] for t in tallies))
+    for k in ARRAY_KEYS:
+        out[k] = np.sum([np.asarray(t[k], dtype=np.int64) for t in tallies], axis=0)
+    return out
+
+
+def tally_vector(t):
+    """Flatten the integer part of a tally for a collective sum."""
+    return np.concatenate([[t[k] for k in INT_KEYS]] + [np.asarray(t[k], dtype=np.int64) for k in ARRAY_KEYS])
+
+
+def tally_from_vector(v, sums=None):
+    v = np.asarray(v, dtype=np.int64)
+    out = {k: int(v[i]) for i, k in enumerate(INT_KEYS)}
+    o = len(INT_KEYS)
+    for k, n in zip(ARRAY_KEYS, (16, 256, 180)):
+        out[k] = v[o:o + n].copy()
+        o += n
+    for k in SUM_KEYS:
+        out[k] = float(sums[k]) if sums else 0.0
+    return out

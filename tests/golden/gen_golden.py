@@ -327,22 +327,22 @@ def _stats_job(args):
             first=(types[0], float(s["pol_angle"][0]), float(s["E_loss"][0])),
             counts=np.bincount(types, minlength=len(c["types"])),
             nan=int(np.isnan(np.asarray(s["pol_angle"], dtype=np.float64)).sum()),
-            # a thinned sample of all events: every 64th
-            sample=np.column_stack([np.asarray(types)[::64],
-                                    np.asarray(s["E"], dtype=np.float64)[::64],
-                                    np.asarray(s["E_loss"], dtype=np.float64)[::64],
-                                    np.asarray(s["pol_angle"], dtype=np.float64)[::64],
-                                    np.asarray(s["az_angle"], dtype=np.float64)[::64]]),
+            # a thinned sample of all events: every 128th
+            sample=np.column_stack([np.asarray(types)[::128],
+                                    np.asarray(s["E"], dtype=np.float64)[::128],
+                                    np.asarray(s["E_loss"], dtype=np.float64)[::128],
+                                    np.asarray(s["pol_angle"], dtype=np.float64)[::128],
+                                    np.asarray(s["az_angle"], dtype=np.float64)[::128]]),
         ))
     return res
 
 
 STATS = [
     # tag, table cfg, tilt, electrons, electrons per job, seed base
-    ("si10", CFG1, 0.0, 20000, 25, 100000),
-    ("au30", CFG3, 70.0, 2000, 5, 200000),
-    ("cu20t45", ("cfg4_Cu_20", "Cu", 20000.0, 1000.0, 100.0, 1e-3), 45.0, 4000, 10, 300000),
-    ("al5", ("cfg4_Al_5", "Al", 5000.0, 1000.0, 100.0, 1e-3), 0.0, 8000, 25, 400000),
+    ("si10", CFG1, 0.0, 30000, 25, 1100000),
+    ("au30", CFG3, 70.0, 3000, 5, 1200000),
+    ("cu20t45", ("cfg4_Cu_20", "Cu", 20000.0, 1000.0, 100.0, 1e-3), 45.0, 12000, 10, 1300000),
+    ("al5", ("cfg4_Al_5", "Al", 5000.0, 1000.0, 100.0, 1e-3), 0.0, 12000, 25, 1400000),
 ]
 
 

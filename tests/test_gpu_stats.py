@@ -91,17 +91,17 @@ def test_first_event_channels_and_angles(golden, tag):
 
 @pytest.mark.parametrize("tag", ["si10", "cu20t45"])
 def test_all_energy_samples(golden, tag):
-    """Every-64th event of the reference against every-64th event here:
+    """Every-128th event of the reference against every-128th event here:
     Rutherford polar angle and inelastic energy losses over all energies
     (reference TestPolarProb_Ruth / TestPolarProb_Moller)."""
     S = golden["ref_stats"]
     p = STATS[tag]
-    n = 8000
+    n = 16000
     g = engine.run(p, num_el=n, seed=5, precision="fp32", ring_capacity=n * 1200)
     ev = g.events
     ev = ev[np.lexsort(((ev["step_chan"] >> 5), ev["electron"]))]
     steps = ev["step_chan"] >> 5
-    ev = ev[steps % 64 == 0]
+    ev = ev[steps % 128 == 0]
     ch = (ev["step_chan"] & 31).astype(int)
     sm = S[tag + "/sample"]
     rch = sm[:, 0].astype(int)
