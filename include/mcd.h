@@ -235,6 +235,24 @@ int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims,
 int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallies,
                     const mcd_tune* tune, uint32_t* status, void* stream);
 
+/* The batched run above without any device allocation, for callers that
+ * cannot call cudaMalloc (an embedding application that owns all device
+ * memory through its own arena; a caller for which an allocation, which can
+ * synchronise the device, would break its latency budget).  No counterpart
+ * in the reference.  Its scratch is a static device array sized for
+ * MCD_STATIC_MAX_SIMS simulations (22.3 KiB), resident on every GPU that
+ * loads the library until exit; more simulations return MCD_ETOOBIG.  The
+ * first call on a device looks up that array's address (issue it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU
+ * race.  The simulations are packed on the host and copied in on `stream`;
+ * tallies[nsims] (zeroed by the caller) and status are device pointers.    */
+#define MCD_STATIC_MAX_SIMS 64
+int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims,
+                            const mcd_material* mats, const int32_t* sim_material,
+                            const mcd_table* tables, const int32_t* sim_moller,
+                            const int32_t* sim_gryz, mcd_tally* tallies,
+                            const mcd_tune* tune, uint32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -406,3 +406,123 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
     k_batched<1><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
+
+// ---------------------------------------------------------------------------
+// Batched run that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: an application that embeds this
+// library and owns all device memory through its own arena, or a caller on a
+// latency budget for which an allocation (which can synchronise the device)
+// is not acceptable.  This variant keeps the batched kernel's scratch (queue
+// counter, electron prefix sums and packed simulation constants) in a
+// file-scope device array instead of a caller workspace.  The array holds at
+// most kStaticMaxSims simulations and stays resident on every GPU that loads
+// the library until the process exits.  Every call shares it and rewrites it
+// in full (the queue counter starts at zero each call), so calls that overlap
+// on the GPU - two streams, or two host threads - race on it and must not be
+// issued concurrently.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace mcd {
+
+constexpr int kStaticMaxSims = MCD_STATIC_MAX_SIMS;
+constexpr size_t kStaticHeadBytes =
+    ((sizeof(BatchHeader) + sizeof(unsigned long long) * (kStaticMaxSims + 1) + 255) / 256) * 256;
+constexpr size_t kStaticScratchBytes = kStaticHeadBytes + sizeof(SimConst<float>) * kStaticMaxSims;
+
+static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
+
+constexpr int kStaticMaxDevices = 64;
+static std::mutex g_static_mu;
+static void* g_static_ptr[kStaticMaxDevices];
+
+// The device address of g_static_scratch on the current device, looked up
+// once per device (host code may not use the symbol itself as an address).
+static int static_scratch(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
+    if (dev < 0 || dev >= kStaticMaxDevices) return MCD_EINVAL;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || !p) return MCD_ECUDA;
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return MCD_OK;
+}
+
+}  // namespace mcd
+
+extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const mcd_material* mats,
+                                       const int32_t* sim_material, const mcd_table* tables,
+                                       const int32_t* sim_moller, const int32_t* sim_gryz, mcd_tally* tallies,
+                                       const mcd_tune* tune, uint32_t* status, void* stream) {
+    if (!sims || !mats || !sim_material || !tallies || !status) return MCD_EINVAL;
+    if (nsims <= 0) return MCD_EINVAL;
+    if (nsims > kStaticMaxSims) return MCD_ETOOBIG;
+    int block = 256, per_sm = 0, refill = 1;
+    if (tune) {
+        if (tune->block_size > 0) block = tune->block_size;
+        if (tune->blocks_per_sm > 0) per_sm = tune->blocks_per_sm;
+        if (tune->refill > 0) refill = tune->refill;
+    }
+    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+
+    // pack on the host stack: header (queue = 0), prefix sums, constants
+    alignas(256) uint8_t host[kStaticScratchBytes];
+    memset(host, 0, kStaticHeadBytes);
+    BatchHeader* h = reinterpret_cast<BatchHeader*>(host);
+    unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + sizeof(BatchHeader));
+    SimConst<float>* cs = reinterpret_cast<SimConst<float>*>(host + kStaticHeadBytes);
+    unsigned long long acc = 0;
+    for (int k = 0; k < nsims; ++k) {
+        const mcd_sim& s = sims[k];
+        const mcd_material& m = mats[sim_material[k]];
+        const mcd_table* tm = nullptr;
+        const mcd_table* tg = nullptr;
+        if (s.mode == MCD_MODE_DS) {
+            if (!tables || !sim_moller || !sim_gryz) return MCD_EINVAL;
+            tm = &tables[sim_moller[k]];
+            tg = &tables[sim_gryz[k]];
+        }
+        const int rc = check_sim(s, m, tm, tg);
+        if (rc != MCD_OK) return rc;
+        if (s.precision != MCD_FP32) return MCD_EINVAL;
+        pre[k] = acc;
+        acc += (unsigned long long)s.num_el;
+        cs[k] = make_consts<float>(s, m, tm, tg);
+    }
+    pre[nsims] = acc;
+    h->queue = 0;
+    h->total = acc;
+    h->nsims = nsims;
+    // the kernel finds the constants at batch_consts_off(nsims); keep that layout
+    if (batch_consts_off(nsims) != kStaticHeadBytes) {
+        memmove(host + batch_consts_off(nsims), cs, sizeof(SimConst<float>) * nsims);
+    }
+    const size_t bytes = batch_bytes(nsims);
+
+    void* scratch = nullptr;
+    int rc = static_scratch(&scratch);
+    if (rc != MCD_OK) return rc;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
+    const size_t smem = batch_smem(nsims);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_batched<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return MCD_ECUDA;
+    int fit = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<1>, block, smem) != cudaSuccess)
+        return MCD_ECUDA;
+    if (fit < 1) return MCD_ETOOBIG;
+    if (per_sm <= 0 || per_sm > fit) per_sm = fit;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // pageable source: the call returns once `host` has been staged, so the
+    // stack buffer may go out of scope afterwards
+    if (cudaMemcpyAsync(scratch, host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) return MCD_ECUDA;
+    k_batched<1><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(scratch), tallies, refill, status);
+    return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
+}

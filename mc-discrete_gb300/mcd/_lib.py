@@ -190,7 +190,11 @@ SIGNATURES = {
                                     C.c_void_p, C.c_size_t, C.c_void_p]),
     "mcd_run_batched": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(Tune), C.c_void_p,
                                   C.c_void_p]),
+    "mcd_run_batched_noalloc": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
+                                          C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                          C.c_void_p, C.POINTER(Tune), C.c_void_p, C.c_void_p]),
 }
+STATIC_MAX_SIMS = 64
 
 _LIB = None
 

@@ -1,0 +1,77 @@
+"""The batched run that allocates nothing (mcd_run_batched_noalloc).
+
+Callers that cannot call cudaMalloc (an application that owns all device
+memory through its own arena, or one whose latency budget cannot absorb an
+allocation that may synchronise the device) use this entry point: its
+scratch lives in a static device array inside the library, and the caller
+passes only inputs and outputs.  It must give the same tallies as the
+workspace-based mcd_batch_prepare + mcd_run_batched, call after call, since
+every call rewrites the shared array.
+
+This file is named to be collected last; it also passes when run alone.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mcd import _lib, engine
+from _gpu_util import input_par
+
+pytestmark = pytest.mark.gpu
+
+SIMS = [
+    dict(input_par("Si", 10000.0, 1000.0, 0.0), num_el=2000),
+    dict(input_par("Au", 20000.0, 1000.0, 45.0), num_el=500),
+    dict(input_par("Cu", 5000.0, 1000.0, 70.0), num_el=3000),
+    dict(input_par("Cu", 20000.0, 1000.0, 70.0, mode="cont", bethe="JL"), num_el=1500),
+]
+
+INT_KEYS = ("none", "bks", "abs", "trsm", "trdf", "long", "events", "double_rows", "nan_events",
+            "clamped", "long_path", "table_range")
+
+
+def _noalloc(b, tune):
+    import torch
+    tallies = torch.zeros_like(b.tallies)
+    status = torch.zeros(1, dtype=torch.int32, device=b.device)
+    st = torch.cuda.current_stream(b.device)
+    code = _lib.lib().mcd_run_batched_noalloc(b._sims_arr, b.n, b.mats, b._idx[0], b._tarr, b._idx[1],
+                                              b._idx[2], tallies.data_ptr(), C.byref(tune),
+                                              status.data_ptr(), st.cuda_stream)
+    _lib.check("mcd_run_batched_noalloc", code)
+    host = tallies.cpu().numpy()
+    return [engine.tally_from_bytes(host[k]) for k in range(b.n)], int(status.item())
+
+
+def _same(a, b):
+    for ta, tb in zip(a, b):
+        for k in INT_KEYS:
+            assert ta[k] == tb[k], k
+        assert np.array_equal(ta["hist_E"], tb["hist_E"])
+        assert np.array_equal(ta["hist_T"], tb["hist_T"])
+        assert abs(ta["sum_E_bks"] - tb["sum_E_bks"]) <= 1e-9 * max(1.0, abs(tb["sum_E_bks"]))
+
+
+def test_noalloc_matches_workspace_run_twice():
+    tune = _lib.Tune(256, 0, 1, 0, 0)
+    b = engine.Batch(SIMS, seed=17)
+    ref, st_ref = b.run(tune)
+    first, st1 = _noalloc(b, tune)
+    second, st2 = _noalloc(b, tune)
+    _same(first, ref)
+    _same(second, ref)
+    assert st1 == st2 == st_ref
+    for t, s in zip(first, SIMS):
+        assert sum(t[o] for o in ("bks", "abs", "trsm", "long")) == s["num_el"]
+
+
+def test_noalloc_rejects_too_many_simulations():
+    b = engine.Batch(SIMS[:1], seed=1)
+    n = _lib.STATIC_MAX_SIMS + 1
+    sims = (_lib.Sim * n)(*([b.structs[0]] * n))
+    idx = (C.c_int32 * n)(*([0] * n))
+    tg = (C.c_int32 * n)(*([1] * n))
+    code = _lib.lib().mcd_run_batched_noalloc(sims, n, b.mats, idx, b._tarr, idx, tg, b.tallies.data_ptr(),
+                                              None, b.status.data_ptr(), None)
+    assert code == _lib.ETOOBIG
