@@ -191,6 +191,50 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+ADJ_WORKLOAD = ("continuous classical Bethe, Al, E0 15 keV, Emin 1 keV, tilt 70 deg, 1e6 electrons, FP32; "
+                "L2 loss of 64 Gaussian-soft exit-energy bins (sigma 50 eV) against a target made with J x 1.1")
+
+
+def adjoint_bench(args, dev):
+    """Forward and adjoint times of the differentiable continuous-mode workload."""
+    import torch
+    from mcd.adjoint import ExitEnergyModel
+    p = dict(material="Al", E0=15000.0, Emin=1000.0, s_tilt=70.0, mode="cont", Bethe_model="classical")
+    n = max(1000, int(round(1e6 * args.scale)))
+    m = ExitEnergyModel(p, n, seed=args.seed, precision="fp32", device=dev)
+    t, _, _ = m.forward(1.1, 1.0)
+    h, _, _ = m.forward(1.0, 1.0)
+    g = 2.0 * (h - t)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        m.launch_forward(1.0, 1.0)
+        m.launch_backward(g, 0.0)
+    torch.cuda.synchronize(dev)
+    tf = tb = 0.0
+    for _ in range(args.steps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        m.launch_forward(1.0, 1.0)
+        e1.record(stream)
+        m.launch_backward(g, 0.0)
+        e2.record(stream)
+        torch.cuda.synchronize(dev)
+        tf += e0.elapsed_time(e1)
+        tb += e1.elapsed_time(e2)
+    h, _, _ = m.forward(1.0, 1.0)
+    L = float(np.sum((h - t) ** 2))
+    dJ, dn = m.backward(2.0 * (h - t), 0.0)
+    d = 1e-3
+    Lp = float(np.sum((m.chain(1 + d, 1.0)[0] - t) ** 2))
+    Lm = float(np.sum((m.chain(1 - d, 1.0)[0] - t) ** 2))
+    fd = (Lp - Lm) / (2 * d)
+    h, _, _ = m.forward(1.0, 1.0)     # restore the checkpoints of J = 1
+    return {"workload": ADJ_WORKLOAD, "num_el": n, "fwd_ms": tf / args.steps, "bwd_ms": tb / args.steps,
+            "bwd_over_fwd": tb / tf, "loss": L, "dL_dJscale": dJ, "dL_dnscale": dn,
+            "fd_frozen_dL_dJscale": fd, "fd_frozen_rel_err": abs(dJ - fd) / abs(fd) if fd else None,
+            "fd_step": d, "gpu_launches": 2 * args.steps}
+
+
 def run_mcd(args):
     import torch
     from mcd import _lib, engine
@@ -332,6 +376,7 @@ def run_mcd(args):
     ach = flop / kt / 1e12
     ach_mufu = mufu / kt / 1e12
 
+    adj = None if args.no_adjoint else adjoint_bench(args, dev)
     if args.no_cpu:
         cpu = {"events": 0, "times": [float("nan")], "threads": 0}
     else:
@@ -361,6 +406,7 @@ def run_mcd(args):
                          "sample": "C oracle, min(num_el, %d) electrons of each sim (%d events)"
                                    % (CPU_SAMPLE_PER_SIM, cpu["events"])},
         "clocks": clk,
+        "adjoint": adj,
         "gpu_launches": K,
         "status": status,
     }
@@ -382,6 +428,7 @@ def main():
                     help="multiply every num_el (profiling of small cases); 1 = the benchmark workload")
     ap.add_argument("--no-plain", action="store_true", help="skip the 64-launch plain path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (bwd/fwd) measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

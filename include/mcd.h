@@ -44,6 +44,8 @@ enum {
 #define MCD_FLAG_LONG_PATH   0x10u /* continuous: a step of 1e4 A or more          */
 #define MCD_FLAG_LONG        0x20u /* an electron reached max_scatt                */
 #define MCD_FLAG_PARKED      0x40u /* batched: electrons left in flight (budget)   */
+#define MCD_FLAG_CKPT        0x80u /* adjoint: an exiting electron had more events
+                                      than checkpoint slots (no gradient)        */
 
 /* ---- enums --------------------------------------------------------------- */
 enum { MCD_OUT_NONE = 0, MCD_OUT_BKS = 1, MCD_OUT_ABS = 2, MCD_OUT_TRSM = 3,
@@ -234,6 +236,50 @@ int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims,
                       size_t workspace_bytes, void* stream);
 int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallies,
                     const mcd_tune* tune, uint32_t* status, void* stream);
+
+/* ---- differentiable continuous mode ------------------------------------- */
+/* Gaussian-soft exit-energy histogram of backscattered electrons:
+ * h_b = (1/num_el) sum exp(-(E_exit - c_b)^2 / (2 sigma^2)),
+ * c_b = lo + (b + 1/2) (hi - lo) / nbins.                                    */
+typedef struct mcd_softhist {
+    int32_t nbins;           /* <= MCD_HIST_E_MAX                             */
+    int32_t reserved;
+    double lo, hi, sigma;    /* eV                                            */
+} mcd_softhist;
+
+/* Per-electron adjoint state (device, caller-owned).                         */
+typedef struct mcd_adjoint_buf {
+    void* ckpt;              /* T [max_ckpt][num_el]: E every 64 events       */
+    int32_t* kstar;          /* [num_el]: exit event of 'bks' electrons or -1 */
+    void* E_exit;            /* T [num_el]: energy of the first outcome row   */
+    int32_t max_ckpt;
+    int32_t reserved;
+} mcd_adjoint_buf;
+
+/* Continuous-mode forward pass that also stores the adjoint checkpoints.
+ * hist_out[nbins + 2] (device, zeroed by the caller) receives the unnormalised
+ * soft bins, the sum of exit energies and the number of 'bks' electrons; tally
+ * (may be NULL) the outcome and event counts.  sim->J_scale and sim->n_scale
+ * scale the Bethe J and the density.  Replaces multiTraj_cont + trajectory_cont_cl
+ * (MC/tools/multiScatter.py:171-229, MC/tools/singleScatter.py:205-239) with
+ * gradients in mind; the reference has no derivative of its own.            */
+int mcd_adjoint_forward(const mcd_sim* sim, const mcd_material* mat, const mcd_softhist* hist,
+                        const mcd_adjoint_buf* buf, double* hist_out, mcd_tally* tally,
+                        uint32_t* status, void* stream);
+
+/* Reverse sweep: grad_hist[nbins + 1] holds dL/dh_b and dL/d(sum of exit
+ * energies); grad[2] (device, zeroed by the caller) receives dL/dJ_scale and
+ * dL/dn_scale, the pathwise derivatives with random numbers and event
+ * sequence frozen.  Each 64-event segment is recomputed from its checkpoint
+ * and the Philox counters.  No counterpart in the reference.                 */
+int mcd_adjoint(const mcd_sim* sim, const mcd_material* mat, const mcd_softhist* hist,
+                const mcd_adjoint_buf* buf, const double* grad_hist, double* grad, void* stream);
+
+/* The exit energies along the frozen event sequence of the last forward pass,
+ * at this call's J_scale / n_scale, as soft bins (for finite-difference checks
+ * of mcd_adjoint).  No counterpart in the reference.                        */
+int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_softhist* hist,
+                      const mcd_adjoint_buf* buf, double* hist_out, void* stream);
 
 /* The batched run above without any device allocation, for callers that
  * cannot call cudaMalloc (an embedding application that owns all device

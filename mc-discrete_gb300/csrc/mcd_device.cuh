@@ -54,6 +54,7 @@ struct Ops<float> {
     static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
     static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
     static __device__ __forceinline__ void sincos_pi(float u, float* s, float* c) {
         __sincosf(3.14159265358979f * u, s, c);
     }
@@ -70,6 +71,7 @@ struct Ops<double> {
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
     static __device__ __forceinline__ double rsqrt_(double x) { return 1.0 / sqrt(x); }
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+    static __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
     static __device__ __forceinline__ void sincos_pi(double u, double* s, double* c) {
         const double a = 3.141592653589793 * u;
         *s = sin(a);
@@ -412,7 +414,9 @@ __device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec,
     }
     const T x0 = L.x, y0 = L.y, z0 = L.z;
     lane_move(L, c, s);
-    T dE = s * stopping<T>(c, E);
+    // a product that is never fused into the energy update, so that the
+    // adjoint's recomputation reproduces these energies bit for bit
+    T dE = Ops<T>::mul_rn(s, stopping<T>(c, E));
     if (!(dE < E)) {
         L.flags |= F_CLAMPED;
         L.clamp_n += 1;

@@ -75,6 +75,8 @@ extern "C" size_t mcd_struct_size(const char* name) {
     if (!strcmp(name, "mcd_event")) return sizeof(mcd_event);
     if (!strcmp(name, "mcd_event_ring")) return sizeof(mcd_event_ring);
     if (!strcmp(name, "mcd_tune")) return sizeof(mcd_tune);
+    if (!strcmp(name, "mcd_softhist")) return sizeof(mcd_softhist);
+    if (!strcmp(name, "mcd_adjoint_buf")) return sizeof(mcd_adjoint_buf);
     return 0;
 }
 

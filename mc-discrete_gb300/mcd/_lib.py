@@ -161,6 +161,16 @@ class Tune(C.Structure):
     ]
 
 
+class SoftHist(C.Structure):
+    _fields_ = [("nbins", C.c_int32), ("reserved", C.c_int32), ("lo", C.c_double), ("hi", C.c_double),
+                ("sigma", C.c_double)]
+
+
+class AdjointBuf(C.Structure):
+    _fields_ = [("ckpt", C.c_void_p), ("kstar", C.c_void_p), ("E_exit", C.c_void_p), ("max_ckpt", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 STRUCTS = {
     "mcd_material": Material,
     "mcd_table": Table,
@@ -170,6 +180,8 @@ STRUCTS = {
     "mcd_event": Event,
     "mcd_event_ring": EventRing,
     "mcd_tune": Tune,
+    "mcd_softhist": SoftHist,
+    "mcd_adjoint_buf": AdjointBuf,
 }
 
 # name -> (restype, argtypes)
@@ -193,8 +205,15 @@ SIGNATURES = {
     "mcd_run_batched_noalloc": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
                                           C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.c_void_p, C.POINTER(Tune), C.c_void_p, C.c_void_p]),
+    "mcd_adjoint_forward": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(SoftHist),
+                                      C.POINTER(AdjointBuf), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mcd_adjoint": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(SoftHist), C.POINTER(AdjointBuf),
+                              C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mcd_adjoint_chain": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(SoftHist),
+                                    C.POINTER(AdjointBuf), C.c_void_p, C.c_void_p]),
 }
 STATIC_MAX_SIMS = 64
+FLAG_CKPT = 0x80
 
 _LIB = None
 

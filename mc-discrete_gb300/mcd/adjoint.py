@@ -1,0 +1,157 @@
+"""Differentiable continuous-mode transport.
+
+ExitEnergyModel runs the continuous-slowing-down transport (mcd_adjoint_forward)
+and keeps, per electron, the energy every 64 events and the event in which it
+left through the surface.  Its backward pass (mcd_adjoint) recomputes each
+64-event segment from the Philox counters and sweeps the energy recursion
+E_{k+1} = E_k - s_k S(E_k) in reverse, giving the pathwise derivatives of
+
+    h_b = (1/N) sum_{bks} exp(-(E_exit - c_b)^2 / (2 sigma^2))   (b < nbins)
+    m   = mean exit energy of backscattered electrons
+
+with respect to the Bethe mean ionisation energy J and the density, both as
+multipliers of the reference values (J_scale, n_scale), with the random
+numbers and the event sequence frozen.
+
+ExitHistogram.apply(J_scale, n_scale, model) wraps it as a torch.autograd
+Function.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .config import with_defaults
+from .engine import make_sim, _torch
+
+
+SoftHist = _lib.SoftHist
+AdjointBuf = _lib.AdjointBuf
+
+
+class ExitEnergyModel:
+    """One continuous-mode simulation whose exit-energy tallies are differentiable."""
+
+    def __init__(self, input_par, num_el, seed=0, nbins=64, sigma=50.0, lo=None, hi=None, precision="fp32",
+                 max_ckpt=64, device="cuda"):
+        torch = _torch()
+        self.p = with_defaults(input_par)
+        if "DS" in self.p["mode"]:
+            self.p["mode"] = "cont"
+        self.n = int(num_el)
+        self.seed = int(seed)
+        self.prec = _lib.FP64 if precision in ("fp64", _lib.FP64) else _lib.FP32
+        self.device = torch.device(device)
+        self.mat = _lib.material(self.p["material"])
+        lo = float(self.p["Emin"]) if lo is None else float(lo)
+        hi = float(self.p["E0"]) if hi is None else float(hi)
+        self.hist = SoftHist(int(nbins), 0, lo, hi, float(sigma))
+        self.nbins = int(nbins)
+        self.max_ckpt = int(max_ckpt)
+        self._alloc()
+        self.last = None   # (J_scale, n_scale) of the stored checkpoints
+
+    def _alloc(self):
+        torch = _torch()
+        dt = torch.float32 if self.prec == _lib.FP32 else torch.float64
+        self.ckpt = torch.empty((self.max_ckpt, self.n), dtype=dt, device=self.device)
+        self.kstar = torch.empty(self.n, dtype=torch.int32, device=self.device)
+        self.E_exit = torch.empty(self.n, dtype=dt, device=self.device)
+        self.buf = AdjointBuf(self.ckpt.data_ptr(), self.kstar.data_ptr(), self.E_exit.data_ptr(), self.max_ckpt, 0)
+        self.hout = torch.zeros(self.nbins + 2, dtype=torch.float64, device=self.device)
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.grad = torch.zeros(2, dtype=torch.float64, device=self.device)
+        self.grad_in = torch.zeros(self.nbins + 1, dtype=torch.float64, device=self.device)
+
+    def sim(self, J_scale, n_scale):
+        return make_sim(self.p, self.n, self.seed, 0, self.prec, 0, J_scale=float(J_scale), n_scale=float(n_scale))
+
+    def _stream(self):
+        torch = _torch()
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def launch_forward(self, J_scale=1.0, n_scale=1.0):
+        """Enqueue the forward pass (no host synchronisation)."""
+        self.hout.zero_()
+        self.status.zero_()
+        s = self.sim(J_scale, n_scale)
+        code = _lib.lib().mcd_adjoint_forward(C.byref(s), C.byref(self.mat), C.byref(self.hist), C.byref(self.buf),
+                                              self.hout.data_ptr(), None, self.status.data_ptr(), self._stream())
+        _lib.check("mcd_adjoint_forward", code)
+        self.last = (float(J_scale), float(n_scale))
+
+    def forward(self, J_scale=1.0, n_scale=1.0):
+        """Soft bins h_b (normalised by N), sum of exit energies, number of 'bks'."""
+        while True:
+            self.launch_forward(J_scale, n_scale)
+            st = int(self.status.item())
+            if not (st & _lib.FLAG_CKPT):   # an exiting electron outran the checkpoint slots
+                break
+            self.max_ckpt *= 2
+            self._alloc()
+        h = self.hout.cpu().numpy()
+        return h[:self.nbins] / self.n, float(h[self.nbins]), float(h[self.nbins + 1])
+
+    def launch_backward(self, grad_h, grad_sum):
+        self.grad.zero_()
+        g = np.concatenate([np.asarray(grad_h, dtype=np.float64).reshape(-1), [float(grad_sum)]])
+        self.grad_in.copy_(_torch().from_numpy(g))
+        s = self.sim(*self.last)
+        code = _lib.lib().mcd_adjoint(C.byref(s), C.byref(self.mat), C.byref(self.hist), C.byref(self.buf),
+                                      self.grad_in.data_ptr(), self.grad.data_ptr(), self._stream())
+        _lib.check("mcd_adjoint", code)
+
+    def backward(self, grad_h, grad_sum=0.0):
+        """(dL/dJ_scale, dL/dn_scale) for dL/dh_b = grad_h, dL/d(sum E_exit) = grad_sum,
+        at the parameters of the last forward pass."""
+        if self.last is None:
+            raise RuntimeError("backward before forward")
+        self.launch_backward(grad_h, grad_sum)
+        g = self.grad.cpu().numpy()
+        return float(g[0]), float(g[1])
+
+    def chain(self, J_scale=1.0, n_scale=1.0):
+        """Soft bins and sum along the frozen event sequence of the last forward pass."""
+        self.hout.zero_()
+        s = self.sim(J_scale, n_scale)
+        code = _lib.lib().mcd_adjoint_chain(C.byref(s), C.byref(self.mat), C.byref(self.hist), C.byref(self.buf),
+                                            self.hout.data_ptr(), self._stream())
+        _lib.check("mcd_adjoint_chain", code)
+        h = self.hout.cpu().numpy()
+        return h[:self.nbins] / self.n, float(h[self.nbins]), float(h[self.nbins + 1])
+
+
+def _function():
+    torch = _torch()
+
+    class ExitHistogram(torch.autograd.Function):
+        """(J_scale, n_scale) -> (soft exit-energy bins [nbins], mean exit energy)."""
+
+        @staticmethod
+        def forward(ctx, J_scale, n_scale, model):
+            h, s, nb = model.forward(float(J_scale), float(n_scale))
+            ctx.model = model
+            ctx.nbks = max(nb, 1.0)
+            dev = J_scale.device
+            return (torch.as_tensor(h, dtype=torch.float64, device=dev),
+                    torch.as_tensor(s / ctx.nbks, dtype=torch.float64, device=dev))
+
+        @staticmethod
+        def backward(ctx, grad_h, grad_m):
+            gh = grad_h.detach().cpu().numpy() if grad_h is not None else np.zeros(ctx.model.nbins)
+            gm = float(grad_m) if grad_m is not None else 0.0
+            dJ, dn = ctx.model.backward(gh, gm / ctx.nbks)
+            return (torch.as_tensor(dJ, dtype=torch.float64), torch.as_tensor(dn, dtype=torch.float64), None)
+
+    return ExitHistogram
+
+
+_FN = None
+
+
+def exit_histogram(J_scale, n_scale, model):
+    """Differentiable (h, mean exit energy) for torch scalars J_scale, n_scale."""
+    global _FN
+    if _FN is None:
+        _FN = _function()
+    return _FN.apply(J_scale, n_scale, model)
