@@ -235,6 +235,34 @@ def adjoint_bench(args, dev):
             "fd_step": d, "gpu_launches": 2 * args.steps}
 
 
+STREAM_WORKLOAD = ("DS Au, E0 30 keV, Emin 0.5 keV, tilt 70 deg, Wc 50 eV, tol 1e-4, every event streamed "
+                   "as a 40-byte record through two device rings to pinned host memory")
+
+
+def stream_bench(args, dev):
+    """Events/s of the streamed DS run, device rings drained to the host."""
+    import torch
+    from mcd.stream import EventStream
+    n = max(10000, int(round(1e7 * args.scale * args.stream_fraction)))
+    p = dict(material="Au", E0=30000.0, Emin=500.0, s_tilt=70.0, Wc=50.0, tol_E=1e-4, tol_W=1e-4, mode="DS",
+             num_el=n)
+    chunk = min(n, 1_000_000)
+    es = EventStream(p, chunk=chunk, seed=args.seed, events_per_electron=950.0, device=dev)
+    seen = [0]
+
+    def consumer(rec, c):            # the host side only counts what arrives
+        seen[0] += rec.size
+
+    es.run(consumer)                  # warm-up pass (tables, rings, pinned buffers)
+    seen[0] = 0
+    torch.cuda.synchronize(dev)
+    st = es.run(consumer)
+    return {"workload": STREAM_WORKLOAD, "num_el": n, "chunk": chunk, "events": st["events"],
+            "records_received": seen[0], "wall_s": st["wall_s"], "events_per_s": st["events"] / st["wall_s"],
+            "drain_GB_per_s": st["bytes"] / st["wall_s"] / 1e9, "ring_GB": es.cap * 40 / 1e9,
+            "reruns": st["reruns"], "gpu_launches": len(es.batches)}
+
+
 def run_mcd(args):
     import torch
     from mcd import _lib, engine
@@ -377,6 +405,7 @@ def run_mcd(args):
     ach_mufu = mufu / kt / 1e12
 
     adj = None if args.no_adjoint else adjoint_bench(args, dev)
+    stream = None if args.no_stream else stream_bench(args, dev)
     if args.no_cpu:
         cpu = {"events": 0, "times": [float("nan")], "threads": 0}
     else:
@@ -407,6 +436,7 @@ def run_mcd(args):
                                    % (CPU_SAMPLE_PER_SIM, cpu["events"])},
         "clocks": clk,
         "adjoint": adj,
+        "stream": stream,
         "gpu_launches": K,
         "status": status,
     }
@@ -429,6 +459,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the 64-launch plain path")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (bwd/fwd) measurement")
+    ap.add_argument("--no-stream", action="store_true", help="skip the streamed-event measurement")
+    ap.add_argument("--stream-fraction", type=float, default=1.0,
+                    help="fraction of the 1e7-electron streaming workload to run (1 = all of it)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

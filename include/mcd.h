@@ -237,6 +237,16 @@ int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims,
 int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallies,
                     const mcd_tune* tune, uint32_t* status, void* stream);
 
+/* The same launch with every event appended to `ring` (device records and
+ * cursor, caller-owned; records at index >= capacity are dropped and show as
+ * cursor > capacity).  The streaming path of the reference's scatter_output
+ * (MC/tools/scattering.py:527-679 via MC/tools/fileTools.py:193-242), which
+ * replaces its per-job pickled lists and HDF5 appends (MC/doScatter.py:99-119).
+ * Event records carry the electron index within its simulation.            */
+int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* tallies,
+                         const mcd_tune* tune, const mcd_event_ring* ring,
+                         uint32_t* status, void* stream);
+
 /* ---- differentiable continuous mode ------------------------------------- */
 /* Gaussian-soft exit-energy histogram of backscattered electrons:
  * h_b = (1/num_el) sum exp(-(E_exit - c_b)^2 / (2 sigma^2)),

@@ -185,9 +185,9 @@ __host__ __device__ inline size_t batch_smem(int nsims) {
            sizeof(BlockTally) * nsims;
 }
 
-template <int MODE_MIX>
+template <int MODE_MIX, bool REC = false>
 __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallies, int refill,
-                                                  uint32_t* status) {
+                                                  uint32_t* status, const mcd_event_ring ring = mcd_event_ring{}) {
     extern __shared__ __align__(16) uint8_t smem[];
     BatchHeader* hdr = reinterpret_cast<BatchHeader*>(ws);
     const int nsims = hdr->nsims;
@@ -247,9 +247,10 @@ __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallie
             EventOut<float> ev;
             int ch;
             if (MODE_MIX == 0 || c.mode == MCD_MODE_DS)
-                ch = ds_event<float, false>(L, c, c.first + local, &ev);
+                ch = ds_event<float, REC>(L, c, c.first + local, &ev);
             else
-                ch = cont_event<float, false>(L, c, c.first + local, &ev);
+                ch = cont_event<float, REC>(L, c, c.first + local, &ev);
+            if (REC && ch >= 0) ring_append(ring, (uint32_t)local, L.step, ev);
             if (ch >= 0 && (c.tally_flags & MCD_TALLY_CHANNELS)) atomicAdd(&s_t[sim].channel[ch], 1u);
             if (L.outcome != MCD_OUT_NONE) {
                 st |= finish_electron(c, L, local, s_t[sim], tallies + sim, eo);
@@ -404,6 +405,41 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
     // reset the queue (the first word of the workspace)
     if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
     k_batched<1><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status);
+    return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
+}
+
+// Batched run that also appends every event to a device ring (the streaming
+// path): the caller drains the ring between launches (mcd.stream).
+extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* tallies, const mcd_tune* tune,
+                                    const mcd_event_ring* ring, uint32_t* status, void* stream) {
+    if (!workspace || !tallies || !status || !ring || !ring->rec || !ring->cursor || ring->capacity == 0)
+        return MCD_EINVAL;
+    if (nsims <= 0) return MCD_EINVAL;
+    if (nsims > kBatchMaxSims) return MCD_ETOOBIG;
+    int block = 256, per_sm = 0, refill = 1;
+    if (tune) {
+        if (tune->block_size > 0) block = tune->block_size;
+        if (tune->blocks_per_sm > 0) per_sm = tune->blocks_per_sm;
+        if (tune->refill > 0) refill = tune->refill;
+    }
+    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
+    const size_t smem = batch_smem(nsims);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(k_batched<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+        return MCD_ECUDA;
+    int fit = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<1, true>, block, smem) != cudaSuccess)
+        return MCD_ECUDA;
+    if (fit < 1) return MCD_ETOOBIG;
+    if (per_sm <= 0 || per_sm > fit) per_sm = fit;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
+    k_batched<1, true><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status,
+                                                          *ring);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 

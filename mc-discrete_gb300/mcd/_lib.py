@@ -205,6 +205,8 @@ SIGNATURES = {
     "mcd_run_batched_noalloc": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
                                           C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.c_void_p, C.POINTER(Tune), C.c_void_p, C.c_void_p]),
+    "mcd_run_batched_ring": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(Tune), C.POINTER(EventRing),
+                                       C.c_void_p, C.c_void_p]),
     "mcd_adjoint_forward": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(SoftHist),
                                       C.POINTER(AdjointBuf), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mcd_adjoint": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(SoftHist), C.POINTER(AdjointBuf),
