@@ -265,7 +265,7 @@ def stream_bench(args, dev):
 
 def run_mcd(args):
     import torch
-    from mcd import _lib, engine
+    from mcd import _lib, autotune, engine, shard
 
     ws, rank, local = dist_env()
     dist = None
@@ -276,10 +276,15 @@ def run_mcd(args):
     dev = torch.device("cuda", local if ws > 1 else 0)
     torch.cuda.set_device(dev)
     sims = workload(args.scale)
-    first = rank << 40            # disjoint Philox electron indices per rank
-    tune = _lib.Tune(args.block, args.blocks_per_sm, args.refill, 0, 0)
+    first = shard.replica_offset(rank)     # disjoint Philox electron indices per rank
 
     batch = engine.Batch(sims, seed=args.seed, device=dev, first_electron=first)
+    if args.block or args.refill:
+        tune = _lib.Tune(args.block or 256, args.blocks_per_sm, args.refill or 1, 0, 0)
+        tune_table = None
+    else:
+        tune, tune_table = autotune.tune(batch)
+    graph = autotune.BatchGraph(batch, tune)
     # plain path: one buffer set per simulation, no per-electron output
     plain = []
     for k, s in enumerate(sims):
@@ -291,9 +296,8 @@ def run_mcd(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def batched_step():
-        batch.zero()
-        batch.launch(tune)
+    def batched_step():                   # zero tallies, reset queue, launch: one graph
+        graph.replay()
 
     def plain_step():
         for sim, mat, tabs, bufs in plain:
@@ -417,8 +421,9 @@ def run_mcd(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * t_batched / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD_NAME, "sims": len(sims), "electrons_per_step": electrons * ws,
-                   "events_per_step": events * ws, "tune": {"block": args.block, "refill": args.refill,
-                                                            "blocks_per_sm": args.blocks_per_sm},
+                   "events_per_step": events * ws,
+                   "tune": {"block": tune.block_size, "refill": tune.refill, "blocks_per_sm": tune.blocks_per_sm,
+                            "autotuned_ms": tune_table, "cuda_graph": True},
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "electrons_per_s": electrons * ws * K / t_batched,
         "plain": {"value": plain_value, "unit": "events/s", "ms_per_step": 1e3 * t_plain / k_plain,
@@ -449,8 +454,8 @@ def main():
     ap.add_argument("--steps", type=int, default=6)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mcd", choices=("mcd", "reference"))
-    ap.add_argument("--block", type=int, default=256)
-    ap.add_argument("--refill", type=int, default=1)
+    ap.add_argument("--block", type=int, default=0, help="batched block size (0: autotune)")
+    ap.add_argument("--refill", type=int, default=0, help="batched refill granularity (0: autotune)")
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--plain-block", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)

@@ -20,11 +20,12 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 1
+#define MCD_ABI_VERSION 2
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
 #define MCD_HIST_T_MAX 180
+#define MCD_GUIDE 32           /* guide entries per table row (see mcd_table) */
 
 /* ---- return codes ------------------------------------------------------ */
 enum {
@@ -98,8 +99,13 @@ typedef struct mcd_table {
     const float* Ws;         /* device, nW energy losses (float32 geomspace)  */
     const float* cdf;        /* device, nE x (nW-1); 0 marks a masked entry   */
     const int32_t* nvalid;   /* device, nE unmasked counts per row, or NULL   */
+    const int32_t* guide;    /* device, nE x (MCD_GUIDE+1): first CDF index
+                                whose value is >= k/MCD_GUIDE, or NULL; it
+                                narrows the search without changing its result */
     int32_t nE;
     int32_t nW;
+    float E_first;           /* Es[0] and Es[nE-1] as the host holds them, so */
+    float E_last;            /* the row guess needs no loads (0: read Es)     */
 } mcd_table;
 
 /* ---- one simulation (the input.file keys, MC/tools/fileTools.py:8-46) ---- */
@@ -201,11 +207,12 @@ int mcd_device_info(int* sm_count, int* cc_major, int* cc_minor);
  * dsigma/dW between consecutive Ws, cumulative sum, normalised by the row
  * total; intervals above Wmax(E) = (E - Ef)/2 are masked (stored as 0).
  * kind is MCD_TABLE_MOLLER (valence electrons, Wmin = Wc) or MCD_TABLE_GRYZ
- * (shell `shell` of the material).  cdf64 and nvalid may be NULL.
+ * (shell `shell` of the material).  cdf64, nvalid and guide may be NULL.
  * Replaces probTable.computeBlock/generate (MC/tools/probTables.py:415-486). */
 int mcd_build_table(int kind, const mcd_material* mat, int shell,
                     int32_t nE, int32_t nW, const float* Es, const float* Ws,
-                    float* cdf32, double* cdf64, int32_t* nvalid, void* stream);
+                    float* cdf32, double* cdf64, int32_t* nvalid, int32_t* guide,
+                    void* stream);
 
 /* One simulation, one GPU thread per electron, one launch.
  * Replaces multiTraj_DS / multiTraj_cont (MC/tools/multiScatter.py:66-116,
@@ -296,7 +303,7 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * memory through its own arena; a caller for which an allocation, which can
  * synchronise the device, would break its latency budget).  No counterpart
  * in the reference.  Its scratch is a static device array sized for
- * MCD_STATIC_MAX_SIMS simulations (22.3 KiB), resident on every GPU that
+ * MCD_STATIC_MAX_SIMS simulations (24.5 KiB), resident on every GPU that
  * loads the library until exit; more simulations return MCD_ETOOBIG.  The
  * first call on a device looks up that array's address (issue it before any
  * stream capture).  Calls share the array: calls that overlap on the GPU

@@ -44,8 +44,10 @@ struct TableDev {
     const float* Ws;
     const float* cdf;
     const int32_t* nvalid;
+    const int32_t* guide;
     int32_t nE;
     int32_t nW;
+    float E_first, E_last;
 };
 
 template <class T>
@@ -151,9 +153,9 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     c.hT = s.hist_T_bins;
     c.invWE = (T)(s.hist_E_width > 0 ? 1.0 / s.hist_E_width : 0.0);
     c.invWT = (T)(s.hist_T_width > 0 ? 1.0 / s.hist_T_width : 0.0);
-    TableDev z{nullptr, nullptr, nullptr, nullptr, 0, 0};
-    c.tm = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->nE, tm->nW} : z;
-    c.tg = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->nE, tg->nW} : z;
+    TableDev z{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0.0f, 0.0f};
+    c.tm = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->guide, tm->nE, tm->nW, tm->E_first, tm->E_last} : z;
+    c.tg = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->guide, tg->nE, tg->nW, tg->E_first, tg->E_last} : z;
     return c;
 }
 

@@ -135,7 +135,8 @@ __device__ __forceinline__ T stopping(const C& c, T E) {
 template <class T>
 __device__ __forceinline__ int table_row(const TableDev& t, T E, bool* out_of_range) {
     const int nE = t.nE;
-    const float e0 = __ldg(t.Es), eL = __ldg(t.Es + nE - 1);
+    const bool known = t.E_last > 0.0f;
+    const float e0 = known ? t.E_first : __ldg(t.Es), eL = known ? t.E_last : __ldg(t.Es + nE - 1);
     if (E > (T)eL) {
         *out_of_range = true;
         return nE - 1;
@@ -168,7 +169,17 @@ __device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) 
     const int i = table_row(t, E, oor);
     const int ncol = t.nW - 1;
     const float* row = t.cdf + (size_t)i * ncol;
-    int lo = 0, hi = t.nvalid ? __ldg(t.nvalid + i) : ncol;
+    int lo, hi;
+    if (t.guide) {
+        // the answer lies between the first entries >= k/G and >= (k+1)/G
+        const int k = (int)(U * (T)MCD_GUIDE);
+        const int32_t* g = t.guide + (size_t)i * (MCD_GUIDE + 1) + k;
+        lo = __ldg(g);
+        hi = __ldg(g + 1);
+    } else {
+        lo = 0;
+        hi = t.nvalid ? __ldg(t.nvalid + i) : ncol;
+    }
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         const float v = __ldg(row + mid);

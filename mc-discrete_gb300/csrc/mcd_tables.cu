@@ -25,6 +25,7 @@ struct FillParams {
     float* cdf32;
     double* cdf64;
     int32_t* nvalid;
+    int32_t* guide;
     int32_t nE, nW;
     int32_t kind;
     double nfree;  // Moller: valence electrons; Gryzinski: shell occupancy
@@ -107,6 +108,22 @@ __global__ void __launch_bounds__(256) k_fill(const FillParams p) {
         }
     }
     if (lane == 0 && p.nvalid) p.nvalid[row] = nval;
+    if (p.guide) {
+        // guide[k] = first entry >= k/G among the unmasked prefix (as the
+        // sampler's bisection sees the row); the row was written by this warp
+        __syncwarp();
+        const float* r = p.cdf32 + (size_t)row * nint;
+        for (int k = lane; k <= MCD_GUIDE; k += 32) {
+            const float q = (float)k / (float)MCD_GUIDE;
+            int lo = 0, hi = nval;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const float v = r[mid];
+                if (v != 0.0f && v < q) lo = mid + 1; else hi = mid;
+            }
+            p.guide[(size_t)row * (MCD_GUIDE + 1) + k] = lo;
+        }
+    }
 }
 
 }  // namespace mcd
@@ -115,7 +132,7 @@ using namespace mcd;
 
 extern "C" int mcd_build_table(int kind, const mcd_material* mat, int shell, int32_t nE, int32_t nW,
                                const float* Es, const float* Ws, float* cdf32, double* cdf64, int32_t* nvalid,
-                               void* stream) {
+                               int32_t* guide, void* stream) {
     if (!mat || !Es || !Ws || !cdf32) return MCD_EINVAL;
     if (nE < 1 || nW < 2) return MCD_EINVAL;
     if (kind != MCD_TABLE_MOLLER && kind != MCD_TABLE_GRYZ) return MCD_EINVAL;
@@ -125,6 +142,7 @@ extern "C" int mcd_build_table(int kind, const mcd_material* mat, int shell, int
     p.cdf32 = cdf32;
     p.cdf64 = cdf64;
     p.nvalid = nvalid;
+    p.guide = guide;
     p.nE = nE;
     p.nW = nW;
     p.kind = kind;

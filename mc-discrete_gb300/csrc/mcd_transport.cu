@@ -171,18 +171,45 @@ struct BatchHeader {
 
 constexpr int kBatchMaxSims = 256;
 
-__host__ __device__ inline size_t batch_prefix_off() { return sizeof(BatchHeader); }
-__host__ __device__ inline size_t batch_consts_off(int nsims) {
-    size_t o = sizeof(BatchHeader) + sizeof(unsigned long long) * (size_t)(nsims + 1);
-    return (o + 255) & ~(size_t)255;
+// Workspace layout: header | prefix[nsims+1] (u64, by queue position) |
+// perm[nsims] (i32: queue position -> simulation) | pad | SimConst[nsims].
+__host__ __device__ constexpr size_t batch_prefix_off() { return sizeof(BatchHeader); }
+__host__ __device__ constexpr size_t batch_perm_off(int nsims) {
+    return sizeof(BatchHeader) + sizeof(unsigned long long) * (size_t)(nsims + 1);
 }
-__host__ __device__ inline size_t batch_bytes(int nsims) {
+__host__ __device__ constexpr size_t batch_consts_off(int nsims) {
+    return (batch_perm_off(nsims) + sizeof(int32_t) * (size_t)nsims + 255) & ~(size_t)255;
+}
+__host__ __device__ constexpr size_t batch_bytes(int nsims) {
     return batch_consts_off(nsims) + sizeof(SimConst<float>) * (size_t)nsims;
 }
 
-__host__ __device__ inline size_t batch_smem(int nsims) {
+__host__ __device__ constexpr size_t batch_smem(int nsims) {
     return sizeof(SimConst<float>) * nsims + sizeof(unsigned long long) * (nsims + 1) +
-           sizeof(BlockTally) * nsims;
+           sizeof(int32_t) * ((nsims + 1) & ~1) + sizeof(BlockTally) * nsims;
+}
+
+// Queue order: simulations with the longest expected trajectories first, so
+// that the last electrons handed out are short ones and the grid drains
+// evenly.  The key is the energy to lose, less for tilted beams (which
+// backscatter more).  Results do not depend on the order: every electron
+// keeps its own (sim, electron, event) Philox counters.
+static void batch_order(const mcd_sim* sims, int nsims, int32_t* perm) {
+    for (int k = 0; k < nsims; ++k) perm[k] = k;
+    auto key = [&](int k) {
+        const double t = sims[k].s_tilt * kPi / 180.0;
+        return (sims[k].E0 - sims[k].Emin) * cos(0.5 * t);
+    };
+    for (int a = 1; a < nsims; ++a) {      // stable insertion sort, descending key
+        const int v = perm[a];
+        const double kv = key(v);
+        int b = a - 1;
+        while (b >= 0 && key(perm[b]) < kv) {
+            perm[b + 1] = perm[b];
+            --b;
+        }
+        perm[b + 1] = v;
+    }
 }
 
 template <int MODE_MIX, bool REC = false>
@@ -194,8 +221,11 @@ __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallie
     const unsigned long long total = hdr->total;
     SimConst<float>* s_c = reinterpret_cast<SimConst<float>*>(smem);
     unsigned long long* s_pre = reinterpret_cast<unsigned long long*>(smem + sizeof(SimConst<float>) * nsims);
+    int32_t* s_perm = reinterpret_cast<int32_t*>(smem + sizeof(SimConst<float>) * nsims +
+                                                 sizeof(unsigned long long) * (nsims + 1));
     BlockTally* s_t = reinterpret_cast<BlockTally*>(smem + sizeof(SimConst<float>) * nsims +
-                                                    sizeof(unsigned long long) * (nsims + 1));
+                                                    sizeof(unsigned long long) * (nsims + 1) +
+                                                    sizeof(int32_t) * ((nsims + 1) & ~1));
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(ws + batch_consts_off(nsims));
         uint32_t* dst = reinterpret_cast<uint32_t*>(s_c);
@@ -203,6 +233,8 @@ __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallie
         for (int k = threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
         const unsigned long long* pre = reinterpret_cast<const unsigned long long*>(ws + batch_prefix_off());
         for (int k = threadIdx.x; k <= nsims; k += blockDim.x) s_pre[k] = pre[k];
+        const int32_t* perm = reinterpret_cast<const int32_t*>(ws + batch_perm_off(nsims));
+        for (int k = threadIdx.x; k < nsims; k += blockDim.x) s_perm[k] = perm[k];
         bt_zero(s_t, nsims);
     }
     __syncthreads();
@@ -225,12 +257,12 @@ __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallie
             if (!have) {
                 const unsigned long long g = base + __popc(idle & lt);
                 if (g < total) {
-                    int lo = 0, hi = nsims;  // s_pre[lo] <= g < s_pre[hi]
+                    int lo = 0, hi = nsims;  // s_pre[lo] <= g < s_pre[hi] (queue positions)
                     while (hi - lo > 1) {
                         const int mid = (lo + hi) >> 1;
                         if (s_pre[mid] <= g) lo = mid; else hi = mid;
                     }
-                    sim = lo;
+                    sim = s_perm[lo];
                     local = g - s_pre[lo];
                     lane_init(L, s_c[sim]);
                     have = true;
@@ -342,8 +374,8 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
     if (!host) return MCD_EINVAL;
     BatchHeader* h = reinterpret_cast<BatchHeader*>(host);
     unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + batch_prefix_off());
+    int32_t* perm = reinterpret_cast<int32_t*>(host + batch_perm_off(nsims));
     SimConst<float>* cs = reinterpret_cast<SimConst<float>*>(host + batch_consts_off(nsims));
-    unsigned long long acc = 0;
     int rc = MCD_OK;
     for (int k = 0; k < nsims && rc == MCD_OK; ++k) {
         const mcd_sim& s = sims[k];
@@ -358,9 +390,13 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
         rc = check_sim(s, m, tm, tg);
         if (rc != MCD_OK) break;
         if (s.precision != MCD_FP32) { rc = MCD_EINVAL; break; }
-        pre[k] = acc;
-        acc += (unsigned long long)s.num_el;
         cs[k] = make_consts<float>(s, m, tm, tg);
+    }
+    batch_order(sims, nsims, perm);
+    unsigned long long acc = 0;
+    for (int q = 0; q < nsims; ++q) {
+        pre[q] = acc;
+        acc += (unsigned long long)sims[perm[q]].num_el;
     }
     pre[nsims] = acc;
     h->queue = 0;
@@ -463,8 +499,7 @@ extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* t
 namespace mcd {
 
 constexpr int kStaticMaxSims = MCD_STATIC_MAX_SIMS;
-constexpr size_t kStaticHeadBytes =
-    ((sizeof(BatchHeader) + sizeof(unsigned long long) * (kStaticMaxSims + 1) + 255) / 256) * 256;
+constexpr size_t kStaticHeadBytes = batch_consts_off(kStaticMaxSims);
 constexpr size_t kStaticScratchBytes = kStaticHeadBytes + sizeof(SimConst<float>) * kStaticMaxSims;
 
 static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
@@ -510,9 +545,9 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     alignas(256) uint8_t host[kStaticScratchBytes];
     memset(host, 0, kStaticHeadBytes);
     BatchHeader* h = reinterpret_cast<BatchHeader*>(host);
-    unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + sizeof(BatchHeader));
-    SimConst<float>* cs = reinterpret_cast<SimConst<float>*>(host + kStaticHeadBytes);
-    unsigned long long acc = 0;
+    unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + batch_prefix_off());
+    int32_t* perm = reinterpret_cast<int32_t*>(host + batch_perm_off(nsims));
+    SimConst<float>* cs = reinterpret_cast<SimConst<float>*>(host + batch_consts_off(nsims));
     for (int k = 0; k < nsims; ++k) {
         const mcd_sim& s = sims[k];
         const mcd_material& m = mats[sim_material[k]];
@@ -526,18 +561,18 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
         const int rc = check_sim(s, m, tm, tg);
         if (rc != MCD_OK) return rc;
         if (s.precision != MCD_FP32) return MCD_EINVAL;
-        pre[k] = acc;
-        acc += (unsigned long long)s.num_el;
         cs[k] = make_consts<float>(s, m, tm, tg);
+    }
+    batch_order(sims, nsims, perm);
+    unsigned long long acc = 0;
+    for (int q = 0; q < nsims; ++q) {
+        pre[q] = acc;
+        acc += (unsigned long long)sims[perm[q]].num_el;
     }
     pre[nsims] = acc;
     h->queue = 0;
     h->total = acc;
     h->nsims = nsims;
-    // the kernel finds the constants at batch_consts_off(nsims); keep that layout
-    if (batch_consts_off(nsims) != kStaticHeadBytes) {
-        memmove(host + batch_consts_off(nsims), cs, sizeof(SimConst<float>) * nsims);
-    }
     const size_t bytes = batch_bytes(nsims);
 
     void* scratch = nullptr;

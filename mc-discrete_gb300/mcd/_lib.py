@@ -9,7 +9,9 @@ import os
 
 from . import build as _build
 
+ABI_VERSION = 2
 MAX_SHELLS = 8
+GUIDE = 32
 MAX_CHANNELS = 16
 HIST_E_MAX = 256
 HIST_T_MAX = 180
@@ -66,8 +68,11 @@ class Table(C.Structure):
         ("Ws", C.c_void_p),
         ("cdf", C.c_void_p),
         ("nvalid", C.c_void_p),
+        ("guide", C.c_void_p),
         ("nE", C.c_int32),
         ("nW", C.c_int32),
+        ("E_first", C.c_float),
+        ("E_last", C.c_float),
     ]
 
 
@@ -192,7 +197,8 @@ SIGNATURES = {
     "mcd_material_init": (C.c_int, [C.c_char_p, C.POINTER(Material)]),
     "mcd_device_info": (C.c_int, [C.POINTER(C.c_int)] * 3),
     "mcd_build_table": (C.c_int, [C.c_int, C.POINTER(Material), C.c_int, C.c_int32, C.c_int32,
-                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
     "mcd_run": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(Table), C.POINTER(Table),
                           C.c_void_p, C.POINTER(ElectronOut), C.POINTER(EventRing), C.c_void_p,
                           C.c_int32, C.c_void_p]),
@@ -242,7 +248,7 @@ def lib(build_if_missing=True):
         f = getattr(h, name)
         f.restype = res
         f.argtypes = args
-    if h.mcd_abi_version() != 1:
+    if h.mcd_abi_version() != ABI_VERSION:
         raise RuntimeError("libmcd ABI version mismatch")
     for name, cls in STRUCTS.items():
         n = h.mcd_struct_size(name.encode())

@@ -72,3 +72,27 @@ def test_batched_rejects_bad_tuning():
         b.launch(_lib.Tune(100, 0, 1, 0, 0))
     with pytest.raises(_lib.MCDError):
         b.launch(_lib.Tune(128, 0, 40, 0, 0))
+
+
+def test_graph_replay_equals_direct_launch():
+    from mcd import autotune
+    b = engine.Batch(SIMS, seed=8)
+    t = _lib.Tune(256, 0, 1, 0, 0)
+    ref, _ = b.run(t)
+    g = autotune.BatchGraph(b, t)
+    for _ in range(2):
+        res, _ = g.run()
+        for a, r in zip(res, ref):
+            for key in INT_KEYS:
+                assert a[key] == r[key], key
+
+
+def test_autotune_picks_a_measured_shape(tmp_path, monkeypatch):
+    from mcd import autotune
+    monkeypatch.setenv("MCD_CACHE_DIR", str(tmp_path))
+    b = engine.Batch(SIMS[:3], seed=4)
+    t, table = autotune.tune(b, fraction=0.2, reps=1, blocks=(128, 256), refills=(1, 8))
+    assert "%d/%d" % (t.block_size, t.refill) in table
+    assert min(table.values()) == table["%d/%d" % (t.block_size, t.refill)]
+    t2, _ = autotune.tune(b)          # from the cache
+    assert (t2.block_size, t2.refill) == (t.block_size, t.refill)

@@ -39,7 +39,7 @@ def test_struct_layouts_match():
 
 def test_abi_and_errors():
     L = _lib.lib()
-    assert L.mcd_abi_version() == 1
+    assert L.mcd_abi_version() == _lib.ABI_VERSION == 2
     assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
     m = _lib.Material()
     assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
@@ -51,7 +51,7 @@ def test_entry_points_reject_bad_arguments_without_touching_the_gpu():
     assert L.mcd_run(None, None, None, None, None, None, None, None, 128, None) == _lib.EINVAL
     assert L.mcd_batch_workspace_bytes(0) == 0
     assert L.mcd_batch_workspace_bytes(257) == 0
-    assert L.mcd_build_table(0, None, 0, 1, 2, None, None, None, None, None, None) == _lib.EINVAL
+    assert L.mcd_build_table(0, None, 0, 1, 2, None, None, None, None, None, None, None) == _lib.EINVAL
     assert L.mcd_run_batched(None, 1, None, None, None, None) == _lib.EINVAL
 
 
@@ -82,10 +82,6 @@ def test_grid_search_fails_like_reference_for_deep_shells():
     """Si 1s at tol 1e-3 has no grid within 1e6 points (the reference raises
     StopIteration); the library raises TableBuildError."""
     m = _lib.material("Si")
-
-    class Inner:
-        pass
-
     spec = tables._Spec("Gryz", m, 10000.0, 1000.0, 100.0, 1e-3, 1e-3)
     spec.Wmin = spec.Eb = 1189.0
     spec.nfree = 2.0
