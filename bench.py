@@ -422,7 +422,8 @@ def run_mcd(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD_NAME, "sims": len(sims), "electrons_per_step": electrons * ws,
                    "events_per_step": events * ws,
-                   "tune": {"block": tune.block_size, "refill": tune.refill, "blocks_per_sm": tune.blocks_per_sm,
+                   "tune": {"block": tune.block_size, "refill": tune.refill, "variant": tune.variant,
+                            "blocks_per_sm": tune.blocks_per_sm,
                             "autotuned_ms": tune_table, "cuda_graph": True},
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "electrons_per_s": electrons * ws * K / t_batched,

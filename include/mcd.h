@@ -186,7 +186,8 @@ typedef struct mcd_tune {
     int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid */
     int32_t refill;          /* idle lanes a warp waits for before it takes
                                 new electrons from the queue (1..32)          */
-    int32_t reserved;
+    int32_t variant;         /* mcd_run_batched: 0 = 64-register kernel, 1 =
+                                48-register kernel (block_size <= 256)        */
     int64_t step_budget;     /* 0 = run to completion; else events per lane
                                 before the kernel parks its electrons         */
 } mcd_tune;

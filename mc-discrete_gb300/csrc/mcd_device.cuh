@@ -91,31 +91,31 @@ __device__ __forceinline__ T sig_ruth(const C& c, T E) {
 }
 
 template <class T, class C>
-__device__ __forceinline__ T sig_moller(const C& c, T E) {
+__device__ __forceinline__ T sig_moller(const C& c, T E, T invE) {
     const T Wc = c.Wc;
     if (!(E > Wc)) return (T)0;
     const T EmW = E - Wc;
-    const T inv = Ops<T>::div((T)1, E * E);
-    return c.pM * inv * (Ops<T>::div(E, Wc) - Ops<T>::div(E, EmW) + Ops<T>::ln(Ops<T>::div(Wc, EmW)));
+    return c.pM * invE * invE * (Ops<T>::div(E, Wc) - Ops<T>::div(E, EmW) + Ops<T>::ln(Ops<T>::div(Wc, EmW)));
 }
 
+// Branch-free: below the binding energy d = 0 makes the value 0 (x = 0), so
+// lanes above and below a threshold run the same instructions.
 template <class T, class C>
-__device__ __forceinline__ T sig_gryz(const C& c, T E, int k) {
+__device__ __forceinline__ T sig_gryz(const C& c, T E, T invE, int k) {
     const T Es = c.gEs[k];
-    if (!(E > Es)) return (T)0;
-    const T d = E - Es;
+    const T d = E > Es ? E - Es : (T)0;
     const T x = Ops<T>::div(d, E + Es);
-    const T br = (T)1 + (T)(2.0 / 3.0) * ((T)1 - (T)0.5 * Es * Ops<T>::div((T)1, E)) *
+    const T br = (T)1 + (T)(2.0 / 3.0) * ((T)1 - (T)0.5 * Es * invE) *
                             Ops<T>::ln((T)2.7 + Ops<T>::sqrt_(d * c.gInvEs[k]));
-    return Ops<T>::div(c.gP[k] * x * Ops<T>::sqrt_(x) * br, E);
+    return c.gP[k] * x * Ops<T>::sqrt_(x) * br * invE;
 }
 
 template <class T, class C>
-__device__ __forceinline__ T sig_quinn(const C& c, T E) {
+__device__ __forceinline__ T sig_quinn(const C& c, T E, T invE) {
     if (!(E > c.Epl)) return (T)0;
     const T a = E * c.qInvEf;
     const T sa = Ops<T>::sqrt_(a), sb = Ops<T>::sqrt_(a - c.qB);
-    return Ops<T>::div(c.qK, E) * Ops<T>::ln(Ops<T>::div(c.qC1 * (sa + sb), c.qB));
+    return c.qK * invE * Ops<T>::ln(Ops<T>::div(c.qC1 * (sa + sb), c.qB));
 }
 
 template <class T, class C>
@@ -328,16 +328,17 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
                            c.key0, c.key1);
     L.step += 1;
     // --- cross sections, channel order Ruth, Moller, Gryz[k], Quinn
+    const T invE = Ops<T>::div((T)1, E);
     const T sR = sig_ruth<T>(c, E);
-    const T sM = sig_moller<T>(c, E);
+    const T sM = sig_moller<T>(c, E, invE);
     T sG[MCD_MAX_SHELLS];
     T tot = sR + sM;
 #pragma unroll
     for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
-        sG[k] = (k < c.nsh) ? sig_gryz<T>(c, E, k) : (T)0;
+        sG[k] = (k < c.nsh) ? sig_gryz<T>(c, E, invE, k) : (T)0;
         tot += sG[k];
     }
-    const T sQ = sig_quinn<T>(c, E);
+    const T sQ = sig_quinn<T>(c, E, invE);
     tot += sQ;
     // --- channel (MC/tools/scattering.py:39-59)
     const T target = Ops<T>::unit(r.x) * tot;

@@ -212,9 +212,28 @@ static void batch_order(const mcd_sim* sims, int nsims, int32_t* perm) {
     }
 }
 
+template <int MODE_MIX, bool REC, int MINB>
+__device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
+                                             const mcd_event_ring& ring);
+
+// Two register budgets of the same kernel: up to 1024 threads per block (64
+// registers, 4 blocks of 256 per SM), or 5 blocks of 256 per SM (48
+// registers, a few spilled values; more warps to hide latency).
 template <int MODE_MIX, bool REC = false>
 __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallies, int refill,
                                                   uint32_t* status, const mcd_event_ring ring = mcd_event_ring{}) {
+    batched_body<MODE_MIX, REC, 0>(ws, tallies, refill, status, ring);
+}
+
+template <int MODE_MIX, bool REC = false>
+__global__ void __launch_bounds__(256, 5) k_batched_lr(uint8_t* ws, mcd_tally* tallies, int refill,
+                                                       uint32_t* status, const mcd_event_ring ring = mcd_event_ring{}) {
+    batched_body<MODE_MIX, REC, 1>(ws, tallies, refill, status, ring);
+}
+
+template <int MODE_MIX, bool REC, int MINB>
+__device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
+                                             const mcd_event_ring& ring) {
     extern __shared__ __align__(16) uint8_t smem[];
     BatchHeader* hdr = reinterpret_cast<BatchHeader*>(ws);
     const int nsims = hdr->nsims;
@@ -423,24 +442,26 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
         if (tune->refill > 0) refill = tune->refill;
     }
     if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+    const bool lowreg = tune && tune->variant == 1;
+    if (lowreg && block > 256) return MCD_EINVAL;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
     const size_t smem = batch_smem(nsims);
+    auto kern = lowreg ? k_batched_lr<1> : k_batched<1>;
     if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(k_batched<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return MCD_ECUDA;
     }
     int fit = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<1>, block, smem) != cudaSuccess)
-        return MCD_ECUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, block, smem) != cudaSuccess) return MCD_ECUDA;
     if (fit < 1) return MCD_ETOOBIG;
     if (per_sm <= 0 || per_sm > fit) per_sm = fit;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // reset the queue (the first word of the workspace)
     if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
-    k_batched<1><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status);
+    kern<<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status,
+                                            mcd_event_ring{});
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 

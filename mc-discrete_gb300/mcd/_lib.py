@@ -161,7 +161,7 @@ class Tune(C.Structure):
         ("block_size", C.c_int32),
         ("blocks_per_sm", C.c_int32),
         ("refill", C.c_int32),
-        ("reserved", C.c_int32),
+        ("variant", C.c_int32),
         ("step_budget", C.c_int64),
     ]
 

@@ -2,7 +2,7 @@
 
 tune(batch) times the kernel on a scaled-down copy of the batch (every
 simulation keeps its parameters; electron counts shrink) for each block size
-x refill granularity, and returns the fastest mcd_tune.  Results are cached
+x refill granularity x register budget, and returns the fastest mcd_tune.  Results are cached
 in a JSON file keyed by the GPU name and a signature of the workload, so a
 later process reuses them without timing.
 
@@ -79,27 +79,28 @@ def tune(batch, fraction=0.1, reps=2, use_cache=True, blocks=BLOCKS, refills=REF
     db = _load() if use_cache else {}
     if key in db:
         c = db[key]
-        return _lib.Tune(c["block"], 0, c["refill"], 0, 0), c.get("table", {})
+        return _lib.Tune(c["block"], 0, c["refill"], c.get("variant", 0), 0), c.get("table", {})
     sims = [dict(p, num_el=max(64, int(round(p["num_el"] * fraction)))) for p in batch.inputs]
     probe = Batch(sims, seed=12345, device=batch.device)
     table = {}
     best = None
     for b in blocks:
         for r in refills:
-            t = _lib.Tune(b, 0, r, 0, 0)
-            try:
-                ms = _time(probe, t, reps)
-            except _lib.MCDError:
-                continue
-            table["%d/%d" % (b, r)] = ms
-            if best is None or ms < best[0]:
-                best = (ms, b, r)
+            for v in ((0, 1) if b <= 256 else (0,)):
+                t = _lib.Tune(b, 0, r, v, 0)
+                try:
+                    ms = _time(probe, t, reps)
+                except _lib.MCDError:
+                    continue
+                table["%d/%d/%d" % (b, r, v)] = ms
+                if best is None or ms < best[0]:
+                    best = (ms, b, r, v)
     if best is None:
         raise RuntimeError("no launch shape fits the batched kernel")
-    db[key] = {"block": best[1], "refill": best[2], "table": table}
+    db[key] = {"block": best[1], "refill": best[2], "variant": best[3], "table": table}
     if use_cache:
         _store(db)
-    return _lib.Tune(best[1], 0, best[2], 0, 0), table
+    return _lib.Tune(best[1], 0, best[2], best[3], 0), table
 
 
 class BatchGraph:

@@ -43,11 +43,12 @@ def plain_tallies():
     return [plain(k, p) for k, p in enumerate(SIMS)]
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("refill", [1, 8, 32])
 @pytest.mark.parametrize("block", [128, 256])
-def test_batched_equals_plain(plain_tallies, refill, block):
+def test_batched_equals_plain(plain_tallies, refill, block, variant):
     b = engine.Batch(SIMS, seed=42)
-    res, status = b.run(_lib.Tune(block, 0, refill, 0, 0))
+    res, status = b.run(_lib.Tune(block, 0, refill, variant, 0))
     for k, (t, ref) in enumerate(zip(res, plain_tallies)):
         for key in INT_KEYS:
             assert t[key] == ref[key], (k, key, t[key], ref[key])
@@ -92,7 +93,7 @@ def test_autotune_picks_a_measured_shape(tmp_path, monkeypatch):
     monkeypatch.setenv("MCD_CACHE_DIR", str(tmp_path))
     b = engine.Batch(SIMS[:3], seed=4)
     t, table = autotune.tune(b, fraction=0.2, reps=1, blocks=(128, 256), refills=(1, 8))
-    assert "%d/%d" % (t.block_size, t.refill) in table
-    assert min(table.values()) == table["%d/%d" % (t.block_size, t.refill)]
+    k = "%d/%d/%d" % (t.block_size, t.refill, t.variant)
+    assert k in table and min(table.values()) == table[k]
     t2, _ = autotune.tune(b)          # from the cache
     assert (t2.block_size, t2.refill) == (t.block_size, t.refill)
