@@ -186,8 +186,10 @@ typedef struct mcd_tune {
     int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid */
     int32_t refill;          /* idle lanes a warp waits for before it takes
                                 new electrons from the queue (1..32)          */
-    int32_t variant;         /* mcd_run_batched: 0 = 64-register kernel, 1 =
-                                48-register kernel (block_size <= 256)        */
+    int32_t variant;         /* bit 0: 48-register kernel (block_size <= 256)
+                                instead of the 64-register one; bit 1: evaluate
+                                cross sections inline instead of from the
+                                tables mcd_batch_prepare builds              */
     int64_t step_budget;     /* 0 = run to completion; else events per lane
                                 before the kernel parks its electrons         */
 } mcd_tune;
@@ -231,7 +233,10 @@ int mcd_run(const mcd_sim* sim, const mcd_material* mat,
 /* Many simulations of uneven size in one persistent launch fed by a global
  * work queue.  mcd_batch_prepare packs the simulations into a caller-owned
  * device workspace of mcd_batch_workspace_bytes(nsims) bytes (host-to-device
- * copy on `stream`; host memory may be reused when the call returns).
+ * copy on `stream`; host memory may be reused when the call returns) and
+ * builds there, per DS simulation, a 4096-point log-energy table of the
+ * cumulative channel cross sections (FP64 evaluation, FP32 storage) that the
+ * kernel interpolates instead of evaluating 3 + n_shells formulas per event.
  * mcd_run_batched then only resets the queue and launches, so it can be
  * captured in a CUDA graph.  tallies[nsims] and status are device pointers.
  * Replaces MapScatterer.__call__ (MC/doScatter.py:54-95) with its pool of

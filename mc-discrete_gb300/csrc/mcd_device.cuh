@@ -315,8 +315,45 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_ph
 // DS event (MC/tools/scattering.py:440-679 in the order of
 // MC/tools/singleScatter.py:15-41).  Returns the channel code.
 // ---------------------------------------------------------------------------
+// Channel and total inverse mean free path from the tabulated cumulative
+// cross sections: linear interpolation in log2(E) between two rows (the
+// table error, about (d ln E)^2 / 8 = 1e-7 relative, is below FP32 rounding).
+template <class C>
+__device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* tot_out) {
+    float t = (__log2f(E) - c.sig_l0) * c.sig_inv;
+    t = fminf(fmaxf(t, 0.0f), (float)(kSigRows - 2) + 0.999f);
+    const int i = (int)t;
+    const float f = t - (float)i;
+    const float* r0 = c.sig + (size_t)i * kSigStride;
+    const float* r1 = r0 + kSigStride;
+    const int K = c.sig_K;
+    const float a = __ldg(r0 + K - 1), b = __ldg(r1 + K - 1);
+    const float tot = fmaf(f, b - a, a);
+    *tot_out = tot;
+    const float target = U * tot;
+    int j = K - 1;
+#pragma unroll
+    for (int q = 0; q < kSigStride / 4; ++q) {
+        const float4 x = __ldg(reinterpret_cast<const float4*>(r0) + q);
+        const float4 y = __ldg(reinterpret_cast<const float4*>(r1) + q);
+        const float v[4] = {fmaf(f, y.x - x.x, x.x), fmaf(f, y.y - x.y, x.y), fmaf(f, y.z - x.z, x.z),
+                            fmaf(f, y.w - x.w, x.w)};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int col = 4 * q + e;
+            if (col < j && target <= v[e]) j = col;
+        }
+    }
+    // column -> channel code: 0 Ruth, 1 Moller, 2..K-2 Gryz[k], K-1 Quinn
+    if (j == 0) return MCD_CH_RUTH;
+    if (j == 1) return MCD_CH_MOLLER;
+    if (j == K - 1) return MCD_CH_QUINN;
+    return MCD_CH_GRYZ0 + (j - 2);
+}
+
 template <class T, bool REC, class C>
-__device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev) {
+__device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev,
+                                        bool use_tab = false) {
     const T E = L.E;
     // --- 'long' check first (MC/tools/singleScatter.py:19-23)
     if (L.step >= c.max_scatt) {
@@ -327,34 +364,41 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
     const uint4 r = philox(make_uint4((uint32_t)L.step, (uint32_t)elec, (uint32_t)(elec >> 32), c.sim_id),
                            c.key0, c.key1);
     L.step += 1;
-    // --- cross sections, channel order Ruth, Moller, Gryz[k], Quinn
-    const T invE = Ops<T>::div((T)1, E);
-    const T sR = sig_ruth<T>(c, E);
-    const T sM = sig_moller<T>(c, E, invE);
-    T sG[MCD_MAX_SHELLS];
-    T tot = sR + sM;
-#pragma unroll
-    for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
-        sG[k] = (k < c.nsh) ? sig_gryz<T>(c, E, invE, k) : (T)0;
-        tot += sG[k];
-    }
-    const T sQ = sig_quinn<T>(c, E, invE);
-    tot += sQ;
-    // --- channel (MC/tools/scattering.py:39-59)
-    const T target = Ops<T>::unit(r.x) * tot;
     int ch = MCD_CH_QUINN;
-    T cum = sR;
-    if (target <= cum) {
-        ch = MCD_CH_RUTH;
+    T tot;
+    if (use_tab) {
+        float tf;
+        ch = tab_pick(c, (float)E, (float)Ops<T>::unit(r.x), &tf);
+        tot = (T)tf;
     } else {
-        cum += sM;
-        if (target <= cum) {
-            ch = MCD_CH_MOLLER;
-        } else {
+        // --- cross sections, channel order Ruth, Moller, Gryz[k], Quinn
+        const T invE = Ops<T>::div((T)1, E);
+        const T sR = sig_ruth<T>(c, E);
+        const T sM = sig_moller<T>(c, E, invE);
+        T sG[MCD_MAX_SHELLS];
+        tot = sR + sM;
 #pragma unroll
-            for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
-                cum += sG[k];
-                if (ch == MCD_CH_QUINN && k < c.nsh && target <= cum) ch = MCD_CH_GRYZ0 + k;
+        for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
+            sG[k] = (k < c.nsh) ? sig_gryz<T>(c, E, invE, k) : (T)0;
+            tot += sG[k];
+        }
+        const T sQ = sig_quinn<T>(c, E, invE);
+        tot += sQ;
+        // --- channel (MC/tools/scattering.py:39-59)
+        const T target = Ops<T>::unit(r.x) * tot;
+        T cum = sR;
+        if (target <= cum) {
+            ch = MCD_CH_RUTH;
+        } else {
+            cum += sM;
+            if (target <= cum) {
+                ch = MCD_CH_MOLLER;
+            } else {
+#pragma unroll
+                for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
+                    cum += sG[k];
+                    if (ch == MCD_CH_QUINN && k < c.nsh && target <= cum) ch = MCD_CH_GRYZ0 + k;
+                }
             }
         }
     }

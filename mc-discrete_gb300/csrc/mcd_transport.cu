@@ -180,8 +180,22 @@ __host__ __device__ constexpr size_t batch_perm_off(int nsims) {
 __host__ __device__ constexpr size_t batch_consts_off(int nsims) {
     return (batch_perm_off(nsims) + sizeof(int32_t) * (size_t)nsims + 255) & ~(size_t)255;
 }
-__host__ __device__ constexpr size_t batch_bytes(int nsims) {
+// ... | FP64 constants (table build only) | cross-section tables.  The no-alloc
+// path copies only the core (up to the FP32 constants) and runs without tables.
+__host__ __device__ constexpr size_t batch_core_bytes(int nsims) {
     return batch_consts_off(nsims) + sizeof(SimConst<float>) * (size_t)nsims;
+}
+__host__ __device__ constexpr size_t batch_dconsts_off(int nsims) {
+    return (batch_core_bytes(nsims) + 255) & ~(size_t)255;
+}
+__host__ __device__ constexpr size_t batch_sig_off(int nsims) {
+    return (batch_dconsts_off(nsims) + sizeof(SimConst<double>) * (size_t)nsims + 255) & ~(size_t)255;
+}
+__host__ __device__ constexpr size_t batch_sig_bytes() {
+    return sizeof(float) * (size_t)kSigRows * kSigStride;
+}
+__host__ __device__ constexpr size_t batch_bytes(int nsims) {
+    return batch_sig_off(nsims) + batch_sig_bytes() * (size_t)nsims;
 }
 
 __host__ __device__ constexpr size_t batch_smem(int nsims) {
@@ -214,26 +228,28 @@ static void batch_order(const mcd_sim* sims, int nsims, int32_t* perm) {
 
 template <int MODE_MIX, bool REC, int MINB>
 __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
-                                             const mcd_event_ring& ring);
+                                             const mcd_event_ring& ring, int inline_sigma);
 
 // Two register budgets of the same kernel: up to 1024 threads per block (64
 // registers, 4 blocks of 256 per SM), or 5 blocks of 256 per SM (48
 // registers, a few spilled values; more warps to hide latency).
 template <int MODE_MIX, bool REC = false>
 __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallies, int refill,
-                                                  uint32_t* status, const mcd_event_ring ring = mcd_event_ring{}) {
-    batched_body<MODE_MIX, REC, 0>(ws, tallies, refill, status, ring);
+                                                  uint32_t* status, const mcd_event_ring ring = mcd_event_ring{},
+                                                  int inline_sigma = 0) {
+    batched_body<MODE_MIX, REC, 0>(ws, tallies, refill, status, ring, inline_sigma);
 }
 
 template <int MODE_MIX, bool REC = false>
 __global__ void __launch_bounds__(256, 5) k_batched_lr(uint8_t* ws, mcd_tally* tallies, int refill,
-                                                       uint32_t* status, const mcd_event_ring ring = mcd_event_ring{}) {
-    batched_body<MODE_MIX, REC, 1>(ws, tallies, refill, status, ring);
+                                                       uint32_t* status, const mcd_event_ring ring = mcd_event_ring{},
+                                                       int inline_sigma = 0) {
+    batched_body<MODE_MIX, REC, 1>(ws, tallies, refill, status, ring, inline_sigma);
 }
 
 template <int MODE_MIX, bool REC, int MINB>
 __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
-                                             const mcd_event_ring& ring) {
+                                             const mcd_event_ring& ring, int inline_sigma) {
     extern __shared__ __align__(16) uint8_t smem[];
     BatchHeader* hdr = reinterpret_cast<BatchHeader*>(ws);
     const int nsims = hdr->nsims;
@@ -298,7 +314,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
             EventOut<float> ev;
             int ch;
             if (MODE_MIX == 0 || c.mode == MCD_MODE_DS)
-                ch = ds_event<float, REC>(L, c, c.first + local, &ev);
+                ch = ds_event<float, REC>(L, c, c.first + local, &ev, !inline_sigma && c.sig != nullptr);
             else
                 ch = cont_event<float, REC>(L, c, c.first + local, &ev);
             if (REC && ch >= 0) ring_append(ring, (uint32_t)local, L.step, ev);
@@ -312,6 +328,32 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
     or_status(status, st);
     __syncthreads();
     for (int k = threadIdx.x; k < nsims; k += blockDim.x) bt_flush(s_t[k], tallies + k);
+}
+
+// Cross-section tables of a prepared batch: one thread per (simulation, grid
+// point), the exact FP64 expressions of the inline path, stored as FP32
+// running sums in pick order.
+__global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)nsims * kSigRows) return;
+    const int s = (int)(gid / kSigRows), i = (int)(gid % kSigRows);
+    const SimConst<double>& c = reinterpret_cast<const SimConst<double>*>(ws + batch_dconsts_off(nsims))[s];
+    const SimConst<float>& cf = reinterpret_cast<const SimConst<float>*>(ws + batch_consts_off(nsims))[s];
+    float* row = reinterpret_cast<float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s) + (size_t)i * kSigStride;
+    const double E = exp2((double)cf.sig_l0 + (double)i / (double)cf.sig_inv);
+    const double invE = 1.0 / E;
+    double cum = sig_ruth<double>(c, E);
+    int col = 0;
+    row[col++] = (float)cum;
+    cum += sig_moller<double>(c, E, invE);
+    row[col++] = (float)cum;
+    for (int k = 0; k < c.nsh; ++k) {
+        cum += sig_gryz<double>(c, E, invE, k);
+        row[col++] = (float)cum;
+    }
+    cum += sig_quinn<double>(c, E, invE);
+    row[col++] = (float)cum;
+    for (; col < kSigStride; ++col) row[col] = 0.0f;
 }
 
 // ---------------------------------------------------------------------------
@@ -388,9 +430,10 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
     if (nsims > kBatchMaxSims) return MCD_ETOOBIG;
     if (workspace_bytes < batch_bytes(nsims)) return MCD_EINVAL;
     if ((reinterpret_cast<uintptr_t>(workspace) & 255) != 0) return MCD_EINVAL;
-    const size_t bytes = batch_bytes(nsims);
+    const size_t bytes = batch_sig_off(nsims);   // everything but the tables, which the GPU fills
     uint8_t* host = static_cast<uint8_t*>(calloc(1, bytes));
     if (!host) return MCD_EINVAL;
+    SimConst<double>* cd = reinterpret_cast<SimConst<double>*>(host + batch_dconsts_off(nsims));
     BatchHeader* h = reinterpret_cast<BatchHeader*>(host);
     unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + batch_prefix_off());
     int32_t* perm = reinterpret_cast<int32_t*>(host + batch_perm_off(nsims));
@@ -410,6 +453,10 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
         if (rc != MCD_OK) break;
         if (s.precision != MCD_FP32) { rc = MCD_EINVAL; break; }
         cs[k] = make_consts<float>(s, m, tm, tg);
+        cd[k] = make_consts<double>(s, m, tm, tg);
+        if (s.mode == MCD_MODE_DS)
+            cs[k].sig = reinterpret_cast<const float*>(static_cast<uint8_t*>(workspace) + batch_sig_off(nsims) +
+                                                       batch_sig_bytes() * k);
     }
     batch_order(sims, nsims, perm);
     unsigned long long acc = 0;
@@ -423,8 +470,12 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
     h->nsims = nsims;
     if (rc == MCD_OK) {
         cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const unsigned grid = (unsigned)(((long long)nsims * kSigRows + 255) / 256);
         if (cudaMemcpyAsync(workspace, host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = MCD_ECUDA;
-        else if (cudaStreamSynchronize(st) != cudaSuccess) rc = MCD_ECUDA;
+        else {
+            k_sigtab<<<grid, 256, 0, st>>>(static_cast<uint8_t*>(workspace), nsims);
+            if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) rc = MCD_ECUDA;
+        }
     }
     free(host);
     return rc;
@@ -442,7 +493,8 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
         if (tune->refill > 0) refill = tune->refill;
     }
     if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
-    const bool lowreg = tune && tune->variant == 1;
+    const bool lowreg = tune && (tune->variant & 1);
+    const int inline_sigma = (tune && (tune->variant & 2)) ? 1 : 0;
     if (lowreg && block > 256) return MCD_EINVAL;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
@@ -461,7 +513,7 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
     // reset the queue (the first word of the workspace)
     if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
     kern<<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status,
-                                            mcd_event_ring{});
+                                            mcd_event_ring{}, inline_sigma);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 
@@ -495,8 +547,9 @@ extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* t
     if (per_sm <= 0 || per_sm > fit) per_sm = fit;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
+    const int inline_sigma = (tune && (tune->variant & 2)) ? 1 : 0;
     k_batched<1, true><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status,
-                                                          *ring);
+                                                          *ring, inline_sigma);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 
@@ -521,7 +574,7 @@ namespace mcd {
 
 constexpr int kStaticMaxSims = MCD_STATIC_MAX_SIMS;
 constexpr size_t kStaticHeadBytes = batch_consts_off(kStaticMaxSims);
-constexpr size_t kStaticScratchBytes = kStaticHeadBytes + sizeof(SimConst<float>) * kStaticMaxSims;
+constexpr size_t kStaticScratchBytes = batch_core_bytes(kStaticMaxSims);
 
 static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
 
@@ -594,7 +647,7 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     h->queue = 0;
     h->total = acc;
     h->nsims = nsims;
-    const size_t bytes = batch_bytes(nsims);
+    const size_t bytes = batch_core_bytes(nsims);   // no cross-section tables: sig stays null
 
     void* scratch = nullptr;
     int rc = static_scratch(&scratch);

@@ -54,7 +54,8 @@ def _same(a, b):
 
 
 def test_noalloc_matches_workspace_run_twice():
-    tune = _lib.Tune(256, 0, 1, 0, 0)
+    # the no-alloc entry evaluates cross sections inline; so does variant bit 1
+    tune = _lib.Tune(256, 0, 1, 2, 0)
     b = engine.Batch(SIMS, seed=17)
     ref, st_ref = b.run(tune)
     first, st1 = _noalloc(b, tune)
