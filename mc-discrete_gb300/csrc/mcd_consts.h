@@ -83,16 +83,20 @@ struct SimConst {
     T invWE, invWT;  // 1/bin width (eV, degrees)
     TableDev tm, tg;
     // cumulative channel cross sections tabulated on a log-E grid (batched
-    // kernel only; nullptr = evaluate inline).  Row i holds, at
-    // E = 2^(sig_l0 + i / sig_inv), the running sums over the channels in
-    // pick order: Ruth, Moller, Gryz[0..nsh-1], Quinn (sig_K = nsh + 3).
+    // kernel only; nullptr = evaluate inline).  Row i (of sig_rows, sig_S
+    // floats apart) holds, at E = 2^(sig_l0 + i / sig_inv), E times the
+    // running sums over the channels in pick order: Ruth, Moller,
+    // Gryz[0..nsh-1], Quinn (sig_K = nsh + 3 columns).  E * sigma varies
+    // slowly in log E, so linear interpolation at 256 rows per octave is
+    // within 2e-7 of the exact sums (relative to the total).
     const float* sig;
-    float sig_l0, sig_inv;
-    int32_t sig_K;
+    float sig_l0, sig_inv, sig_tmax;
+    int32_t sig_K, sig_S, sig_rows;
 };
 
-constexpr int kSigRows = 4096;   // grid points of a cross-section table
-constexpr int kSigStride = 12;   // floats per row (3 + MCD_MAX_SHELLS + 1 = 12)
+constexpr int kSigRowsMax = 4096;      // grid points of a cross-section table, at most
+constexpr int kSigStride = 12;         // floats per row, at most (3 + MCD_MAX_SHELLS + 1)
+constexpr double kSigPerOctave = 256;  // grid density
 
 // Host-side builder: precompute the constant block of one simulation.
 template <class T>
@@ -166,12 +170,12 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     TableDev z{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0.0f, 0.0f};
     c.tm = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->guide, tm->nE, tm->nW, tm->E_first, tm->E_last} : z;
     c.tg = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->guide, tg->nE, tg->nW, tg->E_first, tg->E_last} : z;
-    // grid from just below Emin to just above E0 (the energies an event can start at)
-    const double l0 = log2(s.Emin * (1.0 - 1e-6)), l1 = log2(s.E0 * (1.0 + 1e-6));
+    // no table until a batch shares one among the simulations it fits
     c.sig = nullptr;
-    c.sig_l0 = (float)l0;
-    c.sig_inv = (float)((kSigRows - 1) / (l1 - l0));
+    c.sig_l0 = c.sig_inv = c.sig_tmax = 0.0f;
     c.sig_K = m.n_shells + 3;
+    c.sig_S = (c.sig_K + 3) & ~3;
+    c.sig_rows = 0;
     return c;
 }
 

@@ -143,7 +143,8 @@ __device__ __forceinline__ int table_row(const TableDev& t, T E, bool* out_of_ra
     }
     if (!(E > (T)e0)) return 0;
     // linear-grid guess, then an exact correction against the stored values
-    int g = (int)ceil((double)((E - (T)e0) * (T)(nE - 1) / (T)(eL - e0)));
+    // (computed in T: a guess only, the search below corrects it exactly)
+    int g = (int)ceil((E - (T)e0) * (T)(nE - 1) / (T)(eL - e0));
     g = g < 1 ? 1 : (g > nE - 1 ? nE - 1 : g);
     int lo = 0, hi = nE - 1;  // invariant: Es[lo] < E <= Es[hi]
     for (int it = 0; it < 4; ++it) {
@@ -315,33 +316,36 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_ph
 // DS event (MC/tools/scattering.py:440-679 in the order of
 // MC/tools/singleScatter.py:15-41).  Returns the channel code.
 // ---------------------------------------------------------------------------
-// Channel and total inverse mean free path from the tabulated cumulative
-// cross sections: linear interpolation in log2(E) between two rows (the
-// table error, about (d ln E)^2 / 8 = 1e-7 relative, is below FP32 rounding).
+// Channel and E times the total inverse mean free path from the tabulated
+// cumulative cross sections: linear interpolation in log2(E) between two rows
+// of E * (running sum); the comparison with U * E * total needs no division.
 template <class C>
-__device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* tot_out) {
+__device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Etot_out) {
     float t = (__log2f(E) - c.sig_l0) * c.sig_inv;
-    t = fminf(fmaxf(t, 0.0f), (float)(kSigRows - 2) + 0.999f);
+    t = fminf(fmaxf(t, 0.0f), c.sig_tmax);
     const int i = (int)t;
     const float f = t - (float)i;
-    const float* r0 = c.sig + (size_t)i * kSigStride;
-    const float* r1 = r0 + kSigStride;
+    const int S = c.sig_S;
+    const float* r0 = c.sig + i * S;
+    const float* r1 = r0 + S;
     const int K = c.sig_K;
     const float a = __ldg(r0 + K - 1), b = __ldg(r1 + K - 1);
     const float tot = fmaf(f, b - a, a);
-    *tot_out = tot;
+    *Etot_out = tot;
     const float target = U * tot;
     int j = K - 1;
 #pragma unroll
     for (int q = 0; q < kSigStride / 4; ++q) {
-        const float4 x = __ldg(reinterpret_cast<const float4*>(r0) + q);
-        const float4 y = __ldg(reinterpret_cast<const float4*>(r1) + q);
-        const float v[4] = {fmaf(f, y.x - x.x, x.x), fmaf(f, y.y - x.y, x.y), fmaf(f, y.z - x.z, x.z),
-                            fmaf(f, y.w - x.w, x.w)};
+        if (4 * q < S) {
+            const float4 x = __ldg(reinterpret_cast<const float4*>(r0) + q);
+            const float4 y = __ldg(reinterpret_cast<const float4*>(r1) + q);
+            const float v[4] = {fmaf(f, y.x - x.x, x.x), fmaf(f, y.y - x.y, x.y), fmaf(f, y.z - x.z, x.z),
+                                fmaf(f, y.w - x.w, x.w)};
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int col = 4 * q + e;
-            if (col < j && target <= v[e]) j = col;
+            for (int e = 0; e < 4; ++e) {
+                const int col = 4 * q + e;
+                if (col < j && target <= v[e]) j = col;
+            }
         }
     }
     // column -> channel code: 0 Ruth, 1 Moller, 2..K-2 Gryz[k], K-1 Quinn
@@ -365,18 +369,18 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
                            c.key0, c.key1);
     L.step += 1;
     int ch = MCD_CH_QUINN;
-    T tot;
+    T inv_tot;
     if (use_tab) {
-        float tf;
-        ch = tab_pick(c, (float)E, (float)Ops<T>::unit(r.x), &tf);
-        tot = (T)tf;
+        float Etot;
+        ch = tab_pick(c, (float)E, (float)Ops<T>::unit(r.x), &Etot);
+        inv_tot = Ops<T>::div(E, (T)Etot);
     } else {
         // --- cross sections, channel order Ruth, Moller, Gryz[k], Quinn
         const T invE = Ops<T>::div((T)1, E);
         const T sR = sig_ruth<T>(c, E);
         const T sM = sig_moller<T>(c, E, invE);
         T sG[MCD_MAX_SHELLS];
-        tot = sR + sM;
+        T tot = sR + sM;
 #pragma unroll
         for (int k = 0; k < MCD_MAX_SHELLS; ++k) {
             sG[k] = (k < c.nsh) ? sig_gryz<T>(c, E, invE, k) : (T)0;
@@ -401,9 +405,10 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
                 }
             }
         }
+        inv_tot = Ops<T>::div((T)1, tot);
     }
     // --- path length (MC/tools/scattering.py:551-565)
-    const T s = -Ops<T>::ln_acc(Ops<T>::unit(r.y)) * Ops<T>::div((T)1, tot);
+    const T s = -Ops<T>::ln_acc(Ops<T>::unit(r.y)) * inv_tot;
     const T x0 = L.x, y0 = L.y, z0 = L.z;
     lane_move(L, c, s);
     // --- energy loss and polar angle (MC/tools/scattering.py:568-679)

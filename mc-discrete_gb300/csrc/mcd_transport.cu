@@ -191,8 +191,8 @@ __host__ __device__ constexpr size_t batch_dconsts_off(int nsims) {
 __host__ __device__ constexpr size_t batch_sig_off(int nsims) {
     return (batch_dconsts_off(nsims) + sizeof(SimConst<double>) * (size_t)nsims + 255) & ~(size_t)255;
 }
-__host__ __device__ constexpr size_t batch_sig_bytes() {
-    return sizeof(float) * (size_t)kSigRows * kSigStride;
+__host__ __device__ constexpr size_t batch_sig_bytes() {   // one table slot per simulation
+    return sizeof(float) * (size_t)kSigRowsMax * kSigStride;
 }
 __host__ __device__ constexpr size_t batch_bytes(int nsims) {
     return batch_sig_off(nsims) + batch_sig_bytes() * (size_t)nsims;
@@ -330,30 +330,84 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
     for (int k = threadIdx.x; k < nsims; k += blockDim.x) bt_flush(s_t[k], tallies + k);
 }
 
-// Cross-section tables of a prepared batch: one thread per (simulation, grid
-// point), the exact FP64 expressions of the inline path, stored as FP32
-// running sums in pick order.
+// Cross-section tables of a prepared batch: one thread per (table slot, grid
+// point); a slot is built when its simulation leads a group sharing it.  The
+// exact FP64 expressions of the inline path, stored as FP32 E * running sums
+// in pick order.
 __global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
     const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)nsims * kSigRows) return;
-    const int s = (int)(gid / kSigRows), i = (int)(gid % kSigRows);
-    const SimConst<double>& c = reinterpret_cast<const SimConst<double>*>(ws + batch_dconsts_off(nsims))[s];
+    if (gid >= (long long)nsims * kSigRowsMax) return;
+    const int s = (int)(gid / kSigRowsMax), i = (int)(gid % kSigRowsMax);
     const SimConst<float>& cf = reinterpret_cast<const SimConst<float>*>(ws + batch_consts_off(nsims))[s];
-    float* row = reinterpret_cast<float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s) + (size_t)i * kSigStride;
+    const float* slot = reinterpret_cast<const float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s);
+    if (cf.sig != slot || i >= cf.sig_rows) return;
+    const SimConst<double>& c = reinterpret_cast<const SimConst<double>*>(ws + batch_dconsts_off(nsims))[s];
+    float* row = reinterpret_cast<float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s) + (size_t)i * cf.sig_S;
     const double E = exp2((double)cf.sig_l0 + (double)i / (double)cf.sig_inv);
     const double invE = 1.0 / E;
     double cum = sig_ruth<double>(c, E);
     int col = 0;
-    row[col++] = (float)cum;
+    row[col++] = (float)(E * cum);
     cum += sig_moller<double>(c, E, invE);
-    row[col++] = (float)cum;
+    row[col++] = (float)(E * cum);
     for (int k = 0; k < c.nsh; ++k) {
         cum += sig_gryz<double>(c, E, invE, k);
-        row[col++] = (float)cum;
+        row[col++] = (float)(E * cum);
     }
     cum += sig_quinn<double>(c, E, invE);
-    row[col++] = (float)cum;
-    for (; col < kSigStride; ++col) row[col] = 0.0f;
+    row[col++] = (float)(E * cum);
+    for (; col < cf.sig_S; ++col) row[col] = 0.0f;
+}
+
+// Do two simulations have the same channel cross sections at every energy?
+// (material, Wc and density enter; beam, range and Bethe settings do not)
+inline bool same_sigma(const SimConst<double>& a, const SimConst<double>& b) {
+    if (a.nsh != b.nsh) return false;
+    if (a.cR != b.cR || a.a0 != b.a0 || a.pM != b.pM || a.Wc != b.Wc) return false;
+    if (a.qK != b.qK || a.qC1 != b.qC1 || a.qInvEf != b.qInvEf || a.qB != b.qB || a.Epl != b.Epl) return false;
+    for (int k = 0; k < a.nsh; ++k)
+        if (a.gEs[k] != b.gEs[k] || a.gP[k] != b.gP[k] || a.gInvEs[k] != b.gInvEs[k]) return false;
+    return true;
+}
+
+// Group the DS simulations of a batch by same_sigma; each group shares the
+// table in its first member's slot, on a log2 grid over the union of the
+// members' [Emin, E0] ranges.
+inline void share_sigma_tables(const mcd_sim* sims, int nsims, const SimConst<double>* cd, SimConst<float>* cs,
+                               const uint8_t* ws_dev) {
+    for (int k = 0; k < nsims; ++k) {
+        if (sims[k].mode != MCD_MODE_DS) continue;
+        int lead = k;
+        for (int j = 0; j < k; ++j)
+            if (sims[j].mode == MCD_MODE_DS && cs[j].sig == reinterpret_cast<const float*>(
+                                                                ws_dev + batch_sig_off(nsims) + batch_sig_bytes() * j) &&
+                same_sigma(cd[j], cd[k])) {
+                lead = j;
+                break;
+            }
+        cs[k].sig = reinterpret_cast<const float*>(ws_dev + batch_sig_off(nsims) + batch_sig_bytes() * lead);
+    }
+    for (int k = 0; k < nsims; ++k) {
+        if (sims[k].mode != MCD_MODE_DS) continue;
+        const float* slot = reinterpret_cast<const float*>(ws_dev + batch_sig_off(nsims) + batch_sig_bytes() * k);
+        if (cs[k].sig != slot) continue;
+        double lo = sims[k].Emin, hi = sims[k].E0;
+        for (int j = k + 1; j < nsims; ++j)
+            if (cs[j].sig == slot) {
+                lo = fmin(lo, sims[j].Emin);
+                hi = fmax(hi, sims[j].E0);
+            }
+        const double l0 = log2(lo * (1.0 - 1e-6)), l1 = log2(hi * (1.0 + 1e-6));
+        int rows = (int)ceil((l1 - l0) * kSigPerOctave) + 1;
+        rows = rows < 2 ? 2 : (rows > kSigRowsMax ? kSigRowsMax : rows);
+        for (int j = k; j < nsims; ++j)
+            if (cs[j].sig == slot) {
+                cs[j].sig_l0 = (float)l0;
+                cs[j].sig_inv = (float)((rows - 1) / (l1 - l0));
+                cs[j].sig_tmax = (float)(rows - 2) + 0.999f;
+                cs[j].sig_rows = rows;
+            }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -454,10 +508,8 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
         if (s.precision != MCD_FP32) { rc = MCD_EINVAL; break; }
         cs[k] = make_consts<float>(s, m, tm, tg);
         cd[k] = make_consts<double>(s, m, tm, tg);
-        if (s.mode == MCD_MODE_DS)
-            cs[k].sig = reinterpret_cast<const float*>(static_cast<uint8_t*>(workspace) + batch_sig_off(nsims) +
-                                                       batch_sig_bytes() * k);
     }
+    if (rc == MCD_OK) share_sigma_tables(sims, nsims, cd, cs, static_cast<const uint8_t*>(workspace));
     batch_order(sims, nsims, perm);
     unsigned long long acc = 0;
     for (int q = 0; q < nsims; ++q) {
@@ -470,7 +522,7 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
     h->nsims = nsims;
     if (rc == MCD_OK) {
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        const unsigned grid = (unsigned)(((long long)nsims * kSigRows + 255) / 256);
+        const unsigned grid = (unsigned)(((long long)nsims * kSigRowsMax + 255) / 256);
         if (cudaMemcpyAsync(workspace, host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = MCD_ECUDA;
         else {
             k_sigtab<<<grid, 256, 0, st>>>(static_cast<uint8_t*>(workspace), nsims);

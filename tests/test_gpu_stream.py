@@ -2,17 +2,20 @@
 
 The records streamed chunk by chunk equal those of one run that captures
 every event in a single ring (same Philox electron indices), and a ring too
-small for a chunk is grown and the chunk re-run exactly."""
+small for a chunk is grown and the chunk re-run exactly.  Record-for-record
+equality with the plain kernel needs the batched kernel's inline cross
+sections (tune variant bit 1)."""
 import numpy as np
 import pytest
 
-from mcd import engine
+from mcd import _lib, engine
 from mcd.stream import EventStream
 from _gpu_util import input_par
 
 pytestmark = pytest.mark.gpu
 
 P = dict(input_par("Si", 10000.0, 1000.0, 0.0), num_el=12000)
+INLINE = _lib.Tune(256, 0, 1, 2, 0)
 
 
 def collect_stream(es):
@@ -40,7 +43,7 @@ def single():
 
 def test_stream_equals_single_ring(single):
     ref, g = single
-    es = EventStream(P, chunk=4000, seed=21, events_per_electron=450.0)
+    es = EventStream(P, chunk=4000, seed=21, events_per_electron=450.0, tune=INLINE)
     rec, stats = collect_stream(es)
     assert stats["events"] == stats["events_tallied"] == rec.size == ref.size
     assert stats["reruns"] == 0
@@ -52,8 +55,22 @@ def test_stream_equals_single_ring(single):
 
 def test_stream_regrows_ring_exactly(single):
     ref, _ = single
-    es = EventStream(P, chunk=6000, seed=21, ring_events=100000, piece_bytes=1 << 22)
+    es = EventStream(P, chunk=6000, seed=21, ring_events=100000, piece_bytes=1 << 22, tune=INLINE)
     rec, stats = collect_stream(es)
     assert stats["reruns"] >= 1
     assert rec.size == ref.size
     assert np.array_equal(key(rec)["W"], ref["W"])
+
+
+def test_stream_with_tables_delivers_every_tallied_event(single):
+    ref, _ = single
+    es = EventStream(P, chunk=4000, seed=21, events_per_electron=450.0)
+    rec, stats = collect_stream(es)
+    assert stats["events"] == stats["events_tallied"] == rec.size
+    assert abs(rec.size - ref.size) <= 1e-3 * ref.size
+    # every electron's steps arrive complete and in order 0..n-1
+    rec = key(rec)
+    steps = rec["step_chan"] >> 5
+    first = np.r_[True, rec["electron"][1:] != rec["electron"][:-1]]
+    assert np.all(steps[first] == 0)
+    assert np.all(np.diff(steps)[~first[1:]] == 1)
