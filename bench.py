@@ -235,6 +235,59 @@ def adjoint_bench(args, dev):
             "fd_step": d, "gpu_launches": 2 * args.steps}
 
 
+CONT_WORKLOAD = ("continuous JL Bethe, Cu, E0 20 keV, Emin 1 keV, tilt 70 deg, 1e6 electrons, FP32; "
+                 "exit-energy histogram 200 x 100 eV and polar exit-angle histogram 90 x 1 deg")
+
+
+def cont_bench(args, dev):
+    """Events/s and electrons/s of the continuous-mode histogram workload:
+    one persistent batched launch and one plain launch per step."""
+    import torch
+    from mcd import _lib, engine
+    n = max(1000, int(round(1e6 * args.scale)))
+    p = dict(material="Cu", E0=20000.0, Emin=1000.0, s_tilt=70.0, mode="cont", Bethe_model="JL", num_el=n)
+    b = engine.Batch([p], seed=args.seed, device=dev)
+    tune = _lib.Tune(1024, 0, 1, 0, 0)
+    sim = engine.make_sim(p, n, seed=args.seed)
+    mat = _lib.material("Cu")
+    bufs = engine.RunBuffers(n, _lib.FP32, False, 0, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize(dev)
+        tot = 0.0
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            tot += e0.elapsed_time(e1)
+        return tot / args.steps
+
+    def batched():
+        b.zero()
+        b.launch(tune)
+
+    def plain():
+        bufs.zero()
+        engine.launch(sim, mat, None, bufs, block_size=args.plain_block)
+
+    ms_b = timed(batched)
+    t = b.collect()[0][0]
+    ms_p = timed(plain)
+    tp = engine.collect(bufs).tally
+    ev = int(t["events"])
+    hE = np.asarray(t["hist_E"][:200], dtype=np.float64)
+    mids = (np.arange(200) + 0.5) * 100.0
+    return {"workload": CONT_WORKLOAD, "num_el": n, "events": ev, "ms": ms_b, "events_per_s": ev / ms_b * 1e3,
+            "electrons_per_s": n / ms_b * 1e3, "plain_ms": ms_p, "plain_events_per_s": int(tp["events"]) / ms_p * 1e3,
+            "eta": t["bks"] / n, "mean_exit_E_eV": float((hE * mids).sum() / max(1.0, hE.sum())),
+            "gpu_launches": 2 * args.steps}
+
+
 STREAM_WORKLOAD = ("DS Au, E0 30 keV, Emin 0.5 keV, tilt 70 deg, Wc 50 eV, tol 1e-4, every event streamed "
                    "as a 40-byte record through two device rings to pinned host memory")
 
@@ -410,6 +463,7 @@ def run_mcd(args):
 
     adj = None if args.no_adjoint else adjoint_bench(args, dev)
     stream = None if args.no_stream else stream_bench(args, dev)
+    cont = None if args.no_cont else cont_bench(args, dev)
     if args.no_cpu:
         cpu = {"events": 0, "times": [float("nan")], "threads": 0}
     else:
@@ -443,6 +497,7 @@ def run_mcd(args):
         "clocks": clk,
         "adjoint": adj,
         "stream": stream,
+        "cont": cont,
         "gpu_launches": K,
         "status": status,
     }
@@ -466,6 +521,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (bwd/fwd) measurement")
     ap.add_argument("--no-stream", action="store_true", help="skip the streamed-event measurement")
+    ap.add_argument("--no-cont", action="store_true", help="skip the continuous-mode histogram measurement")
     ap.add_argument("--stream-fraction", type=float, default=1.0,
                     help="fraction of the 1e7-electron streaming workload to run (1 = all of it)")
     args = ap.parse_args()

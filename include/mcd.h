@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 2
+#define MCD_ABI_VERSION 3
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -52,8 +52,16 @@ enum {
 enum { MCD_OUT_NONE = 0, MCD_OUT_BKS = 1, MCD_OUT_ABS = 2, MCD_OUT_TRSM = 3,
        MCD_OUT_TRDF = 4, MCD_OUT_LONG = 5 };
 /* channels: Rutherford, Moller, Quinn, then Gryzinski shell k = 3 + k in the
- * material's shell order (MC/tools/scattering.py:483-508)                   */
-enum { MCD_CH_RUTH = 0, MCD_CH_MOLLER = 1, MCD_CH_QUINN = 2, MCD_CH_GRYZ0 = 3 };
+ * material's shell order (MC/tools/scattering.py:483-508), and diffraction
+ * (diffMFP, :510-516)                                                        */
+enum { MCD_CH_RUTH = 0, MCD_CH_MOLLER = 1, MCD_CH_QUINN = 2, MCD_CH_GRYZ0 = 3, MCD_CH_DIFF = 11 };
+/* elastic total cross section (MC/tools/crossSections.py:37-147); the polar
+ * angle is always drawn with the Rutherford screening alpha
+ * (MC/tools/scattering.py:125-152, :575)                                     */
+enum { MCD_ELASTIC_RUTH = 0,         /* 'Ruth_vanilla'                       */
+       MCD_ELASTIC_RUTH_WDEFL = 1,   /* 'Ruth_vanilla_wDefl': Z^2 -> Z(Z+1)   */
+       MCD_ELASTIC_NIGRAM = 2,       /* 'Ruth_nigram'                         */
+       MCD_ELASTIC_NIGRAM_WDEFL = 3  /* 'Ruth_nigram_wDefl'                   */ };
 enum { MCD_MODE_DS = 0, MCD_MODE_CONT = 1 };
 enum { MCD_BETHE_CLASSICAL = 0, MCD_BETHE_JL = 1, MCD_BETHE_EXPLICIT = 2 };
 enum { MCD_FP32 = 0, MCD_FP64 = 1 };
@@ -91,6 +99,8 @@ typedef struct mcd_material {
     double J;                        /* Bethe mean ionisation energy, eV      */
     double shell_E[MCD_MAX_SHELLS];  /* binding energies, eV                  */
     double shell_n[MCD_MAX_SHELLS];  /* occupancies                           */
+    double xip_g;                    /* extinction distance of the diffraction
+                                        channel (0: none; Si 1360)            */
 } mcd_material;
 
 /* ---- sampled CDF table (MC/tools/probTables.py:70-162, 490-535) ---------- */
@@ -130,6 +140,13 @@ typedef struct mcd_sim {
     double hist_T_width;     /* degrees per bin                               */
     double J_scale;          /* continuous: Bethe J multiplier (1 = reference)*/
     double n_scale;          /* density multiplier (1 = reference)            */
+    int32_t elastic;         /* MCD_ELASTIC_*                                 */
+    int32_t diff_mfp;        /* DS: diffraction channel of constant cross
+                                section 1/(n xip_g) m^3/nm/cm^2; its step has
+                                mean free path xip_g, no loss, no deflection,
+                                and crossing the bottom face on that step is
+                                'trdf' (MC/tools/scattering.py:510-548,658-668,
+                                MC/tools/electron.py:72-79); needs xip_g > 0 */
 } mcd_sim;
 
 /* ---- per-simulation tallies (device, caller zeroes them) ----------------- */

@@ -82,8 +82,9 @@ __device__ __forceinline__ void stopping_derivs(const C& c, T E, T* S, T* SE, T*
 // d ln(sigma'_R)/dE
 template <class T, class C>
 __device__ __forceinline__ T dlnsig(const C& c, T E) {
-    return (T)2 * (Ops<T>::div((T)1, E + (T)511000) - Ops<T>::div((T)1, E + (T)1024000)) -
-           Ops<T>::div((T)1, E + c.a0);
+    const T rel = c.ruth_r2 ? (T)2 * (Ops<T>::div((T)1, E + (T)511000) - Ops<T>::div((T)1, E + (T)1024000))
+                            : (T)0;
+    return rel - Ops<T>::div((T)1, E + c.aS);
 }
 
 template <class T>

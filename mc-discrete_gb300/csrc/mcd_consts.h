@@ -9,6 +9,13 @@
 //  Rutherford (MC/tools/crossSections.py:14-58), alpha = a0 / E,
 //     sigma' = cR * r^2 / (E + a0),  r = (E + 511000) / (E + 1024000),
 //     cR = 5.21e-21 * 1e6 * 4 pi Z^2 / a0 * n * 1e-14,  a0 = 3.4 Z^0.666667
+//     (wDefl, :63-86: Z^2 -> Z (Z + 1))
+//  Nigram (crossSections.py:90-147), beta* = b / E, b = 0.48 * 5.43 Z^(2/3),
+//     sigma' = cN / (E + b),  cN = pi e^4 Z^2 / (4 b) * n * 1e-14
+//     (wDefl: Z^2 -> Z (Z + 1)); no r^2 factor
+//  diffraction (crossSections.py:329-349), sigma = 1e13 / (n xip_g) cm^2,
+//     sigma' = 0.1 / xip_g, and the step of a diffraction event has mean
+//     free path xip_g (scattering.py:540-548)
 //  Moller (crossSections.py:183-208), E > Wc,
 //     sigma' = pM / E^2 * (E/Wc - E/(E-Wc) + ln(Wc/(E-Wc))),
 //     pM = n_val * pi e^4 * n * 1e-14
@@ -55,8 +62,13 @@ struct SimConst {
     // transport
     T E0, Emin, thickness;
     T d0x, d0y, d0z;
-    // Rutherford
-    T cR, a0;
+    // Rutherford: cR, a0 of the default model; the elastic total cross
+    // section is sigma' = cRs * (ruth_r2 ? r^2 : 1) / (E + aS), and the polar
+    // angle always uses a0
+    T cR, a0, cRs, aS;
+    int32_t ruth_r2;
+    int32_t diff;   // diffraction channel on (DS)
+    T dS, xip;      // its sigma' (1/A) and step mean free path (A)
     // Moller
     T pM, Wc;
     // Gryzinski shells
@@ -115,6 +127,21 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     const double a0 = 3.4 * pow(Z, 0.666667);
     c.a0 = (T)a0;
     c.cR = (T)(5.21e-21 * 1e6 * 4.0 * kPi * Z * Z / a0 * n * 1e-14);
+    const bool wdefl = s.elastic == MCD_ELASTIC_RUTH_WDEFL || s.elastic == MCD_ELASTIC_NIGRAM_WDEFL;
+    const double zz = wdefl ? Z * (Z + 1.0) : Z * Z;
+    if (s.elastic == MCD_ELASTIC_NIGRAM || s.elastic == MCD_ELASTIC_NIGRAM_WDEFL) {
+        const double b = 0.48 * 5.43 * pow(Z, 2.0 / 3.0);
+        c.aS = (T)b;
+        c.cRs = (T)(kPiEfour * zz / (4.0 * b) * n * 1e-14);
+        c.ruth_r2 = 0;
+    } else {
+        c.aS = (T)a0;
+        c.cRs = wdefl ? (T)(5.21e-21 * 1e6 * 4.0 * kPi * zz / a0 * n * 1e-14) : c.cR;
+        c.ruth_r2 = 1;
+    }
+    c.diff = (s.mode == MCD_MODE_DS && s.diff_mfp) ? 1 : 0;
+    c.dS = (T)(c.diff ? 0.1 / m.xip_g : 0.0);
+    c.xip = (T)(c.diff ? m.xip_g : 0.0);
     c.pM = (T)(m.n_val * kPiEfour * n * 1e-14);
     c.Wc = (T)s.Wc;
     c.nsh = m.n_shells;
@@ -185,6 +212,8 @@ inline int check_sim(const mcd_sim& s, const mcd_material& m, const mcd_table* t
     if (s.mode != MCD_MODE_DS && s.mode != MCD_MODE_CONT) return MCD_EINVAL;
     if (s.mode == MCD_MODE_CONT && (s.bethe_model < 0 || s.bethe_model > 2)) return MCD_EINVAL;
     if (s.precision != MCD_FP32 && s.precision != MCD_FP64) return MCD_EINVAL;
+    if (s.elastic < MCD_ELASTIC_RUTH || s.elastic > MCD_ELASTIC_NIGRAM_WDEFL) return MCD_EINVAL;
+    if (s.diff_mfp && (s.mode != MCD_MODE_DS || !(m.xip_g > 0))) return MCD_EINVAL;
     if (!(s.E0 > s.Emin) || !(s.Emin > 0)) return MCD_EINVAL;
     if (s.num_el < 0) return MCD_EINVAL;
     if (m.n_shells < 0 || m.n_shells > MCD_MAX_SHELLS || m.atnd <= 0) return MCD_EINVAL;

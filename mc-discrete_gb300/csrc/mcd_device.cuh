@@ -86,8 +86,12 @@ struct Ops<double> {
 // ---------------------------------------------------------------------------
 template <class T, class C>
 __device__ __forceinline__ T sig_ruth(const C& c, T E) {
-    const T r = Ops<T>::div(E + (T)511000, E + (T)1024000);
-    return Ops<T>::div(c.cR * r * r, E + c.a0);
+    T f = c.cRs;
+    if (c.ruth_r2) {
+        const T r = Ops<T>::div(E + (T)511000, E + (T)1024000);
+        f = c.cRs * r * r;
+    }
+    return Ops<T>::div(f, E + c.aS);
 }
 
 template <class T, class C>
@@ -192,7 +196,8 @@ __device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) 
 // ---------------------------------------------------------------------------
 // electron state
 // ---------------------------------------------------------------------------
-enum : uint32_t { F_DOUBLE_ROW = 1u, F_NAN = 2u, F_TABLE_RANGE = 4u, F_CLAMPED = 8u, F_LONG_PATH = 16u };
+enum : uint32_t { F_DOUBLE_ROW = 1u, F_NAN = 2u, F_TABLE_RANGE = 4u, F_CLAMPED = 8u, F_LONG_PATH = 16u,
+                  F_DIFFRACTING = 32u };
 
 template <class T>
 struct Lane {
@@ -230,7 +235,8 @@ struct EventOut {
     int ch;
 };
 
-// Position update and the exit tests (MC/tools/electron.py:64-84).
+// Position update and the exit tests (MC/tools/electron.py:64-84): leaving
+// through the bottom face on a diffraction event's step is 'trdf'.
 template <class T, class C>
 __device__ __forceinline__ void lane_move(Lane<T>& L, const C& c, T s) {
     const T nz = L.z + s * L.dz;
@@ -238,7 +244,7 @@ __device__ __forceinline__ void lane_move(Lane<T>& L, const C& c, T s) {
         L.outcome = MCD_OUT_BKS;
         L.E_row = L.E;
     } else if (nz >= c.thickness) {
-        L.outcome = MCD_OUT_TRSM;
+        L.outcome = (L.flags & F_DIFFRACTING) ? MCD_OUT_TRDF : MCD_OUT_TRSM;
         L.E_row = L.E;
     } else {
         L.x += s * L.dx;
@@ -331,8 +337,10 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     const int K = c.sig_K;
     const float a = __ldg(r0 + K - 1), b = __ldg(r1 + K - 1);
     const float tot = fmaf(f, b - a, a);
-    *Etot_out = tot;
-    const float target = U * tot;
+    const float all = fmaf(E, c.dS, tot);   // + diffraction (dS = 0 when off)
+    *Etot_out = all;
+    const float target = U * all;
+    if (c.diff && target > tot) return MCD_CH_DIFF;
     int j = K - 1;
 #pragma unroll
     for (int q = 0; q < kSigStride / 4; ++q) {
@@ -388,6 +396,8 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
         }
         const T sQ = sig_quinn<T>(c, E, invE);
         tot += sQ;
+        const T cumQ = tot;
+        if (c.diff) tot += c.dS;
         // --- channel (MC/tools/scattering.py:39-59)
         const T target = Ops<T>::unit(r.x) * tot;
         T cum = sR;
@@ -403,12 +413,16 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
                     cum += sG[k];
                     if (ch == MCD_CH_QUINN && k < c.nsh && target <= cum) ch = MCD_CH_GRYZ0 + k;
                 }
+                if (c.diff && ch == MCD_CH_QUINN && target > cumQ) ch = MCD_CH_DIFF;
             }
         }
         inv_tot = Ops<T>::div((T)1, tot);
     }
-    // --- path length (MC/tools/scattering.py:551-565)
-    const T s = -Ops<T>::ln_acc(Ops<T>::unit(r.y)) * inv_tot;
+    // --- path length (MC/tools/scattering.py:540-565): a diffraction event
+    // steps with mean free path xip_g and marks the electron diffracting
+    const bool diff_ev = ch == MCD_CH_DIFF;
+    L.flags = diff_ev ? (L.flags | F_DIFFRACTING) : (L.flags & ~F_DIFFRACTING);
+    const T s = -Ops<T>::ln_acc(Ops<T>::unit(r.y)) * (diff_ev ? c.xip : inv_tot);
     const T x0 = L.x, y0 = L.y, z0 = L.z;
     lane_move(L, c, s);
     // --- energy loss and polar angle (MC/tools/scattering.py:568-679)
@@ -419,6 +433,10 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
         s2 = Ops<T>::div(a * Ops<T>::unit(r.z), a + Ops<T>::unit_c(r.z));
     } else if (ch == MCD_CH_QUINN) {
         W = c.Epl;
+        s2 = (T)0;
+    } else if (diff_ev) {
+        // no loss, no deflection (MC/tools/scattering.py:658-668)
+        W = (T)0;
         s2 = (T)0;
     } else {
         bool oor = false;

@@ -28,19 +28,20 @@ struct SpeciesSpec {
     const char* name_val;
     int Z;
     double n_val, E_val, density, atwt, bethe_k;
+    double xip_g;  // extinction distance (0,0,4) at 20 keV, material.py:225-226; 0 = none
     int n_shells;
     ShellSpec shells[MCD_MAX_SHELLS];
 };
 
 // MC/tools/material.py:151-302 (shell order = the reference's name_s order)
 const SpeciesSpec kSpecies[] = {
-    {"Al", "3s2-3p1", 13, 3, 72.55, 2.70, 26.98154, 0.815, 3,
+    {"Al", "3s2-3p1", 13, 3, 72.55, 2.70, 26.98154, 0.815, 0.0, 3,
      {{"1s", 1559.0, 2}, {"2s", 118.0, 2}, {"2p", 73.5, 6}}},
-    {"Si", "3s2-3p2", 14, 4, 99.42, 2.33, 28.085, 0.822, 3,
+    {"Si", "3s2-3p2", 14, 4, 99.42, 2.33, 28.085, 0.822, 1360.0, 3,
      {{"1s", 1189.0, 2}, {"2s", 149.0, 2}, {"2p", 100.0, 6}}},
-    {"Cu", "3d10-4s2", 29, 11, 75.1, 8.96, 63.546, 0.83, 4,
+    {"Cu", "3d10-4s2", 29, 11, 75.1, 8.96, 63.546, 0.83, 0.0, 4,
      {{"1s", 8980.0, 2}, {"2s2p", 977.0, 8}, {"3s", 120.0, 2}, {"3p", 74.0, 6}}},
-    {"Au", "5d10-6s1", 79, 11, 75.1, 19.30, 196.967, 0.851, 8,
+    {"Au", "5d10-6s1", 79, 11, 75.1, 19.30, 196.967, 0.851, 0.0, 8,
      {{"2s2p", 12980.0, 8}, {"3s3p3d", 2584.0, 18}, {"4s4p", 624.0, 8}, {"4d", 341.0, 10},
       {"5s", 178.0, 2}, {"4f", 85.0, 14}, {"5p2", 72.0, 2}, {"5p4", 54.0, 4}}},
 };
@@ -98,6 +99,7 @@ extern "C" int mcd_material_init(const char* species, mcd_material* out) {
     out->density = s->density;
     out->atwt = s->atwt;
     out->bethe_k = s->bethe_k;
+    out->xip_g = s->xip_g;
     for (int k = 0; k < s->n_shells; ++k) {
         copy_name(out->shell_name[k], sizeof(out->shell_name[k]), s->shells[k].name);
         out->shell_E[k] = s->shells[k].E;

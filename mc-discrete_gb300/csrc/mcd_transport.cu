@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
 // (material, Wc and density enter; beam, range and Bethe settings do not)
 inline bool same_sigma(const SimConst<double>& a, const SimConst<double>& b) {
     if (a.nsh != b.nsh) return false;
-    if (a.cR != b.cR || a.a0 != b.a0 || a.pM != b.pM || a.Wc != b.Wc) return false;
+    if (a.cRs != b.cRs || a.aS != b.aS || a.ruth_r2 != b.ruth_r2 || a.pM != b.pM || a.Wc != b.Wc) return false;
     if (a.qK != b.qK || a.qC1 != b.qC1 || a.qInvEf != b.qInvEf || a.qB != b.qB || a.Epl != b.Epl) return false;
     for (int k = 0; k < a.nsh; ++k)
         if (a.gEs[k] != b.gEs[k] || a.gP[k] != b.gP[k] || a.gInvEs[k] != b.gInvEs[k]) return false;

@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_SHELLS = 8
 GUIDE = 32
 MAX_CHANNELS = 16
@@ -28,7 +28,10 @@ FLAG_PARKED = 0x40
 
 OUT_NONE, OUT_BKS, OUT_ABS, OUT_TRSM, OUT_TRDF, OUT_LONG = range(6)
 OUTCOME_NAMES = ("none", "bks", "abs", "trsm", "trdf", "long")
-CH_RUTH, CH_MOLLER, CH_QUINN, CH_GRYZ0 = 0, 1, 2, 3
+CH_RUTH, CH_MOLLER, CH_QUINN, CH_GRYZ0, CH_DIFF = 0, 1, 2, 3, 11
+ELASTIC_RUTH, ELASTIC_RUTH_WDEFL, ELASTIC_NIGRAM, ELASTIC_NIGRAM_WDEFL = 0, 1, 2, 3
+ELASTIC = {"Ruth_vanilla": ELASTIC_RUTH, "Ruth_vanilla_wDefl": ELASTIC_RUTH_WDEFL,
+           "Ruth_nigram": ELASTIC_NIGRAM, "Ruth_nigram_wDefl": ELASTIC_NIGRAM_WDEFL}
 MODE_DS, MODE_CONT = 0, 1
 BETHE = {"classical": 0, "JL": 1, "explicit": 2}
 FP32, FP64 = 0, 1
@@ -59,6 +62,7 @@ class Material(C.Structure):
         ("J", C.c_double),
         ("shell_E", C.c_double * MAX_SHELLS),
         ("shell_n", C.c_double * MAX_SHELLS),
+        ("xip_g", C.c_double),
     ]
 
 
@@ -99,6 +103,8 @@ class Sim(C.Structure):
         ("hist_T_width", C.c_double),
         ("J_scale", C.c_double),
         ("n_scale", C.c_double),
+        ("elastic", C.c_int32),
+        ("diff_mfp", C.c_int32),
     ]
 
 

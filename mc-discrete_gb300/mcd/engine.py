@@ -32,9 +32,47 @@ def mode_of(input_par):
     return _lib.MODE_DS if "DS" in input_par.get("mode", "DS") else _lib.MODE_CONT
 
 
+def elastic_model(elastic, mode, dispatch="reference"):
+    """The MCD_ELASTIC_* code of an input.file 'elastic' value.
+
+    dispatch="reference" follows the reference's string tests:
+      DS (MC/tools/scattering.py:483-493): 'Ruth_vanilla' exactly; any name
+        containing 'vanilla_wDefl' calls ruther_sigma_wDefl, which that module
+        never imports (:14), so it raises NameError; 'Ruth_nigram' exactly;
+        any name containing 'nigram_wDefl'.
+      continuous (:781-790): any name containing 'vanilla', then any name
+        containing 'nigram' -- so both wDefl variants fall back to their
+        base models.
+    dispatch="intended" maps the four names one to one.  Names containing
+    'Ruth' that match no rule (the reference then runs without an elastic
+    channel) raise ValueError; other names select Mott scattering, whose
+    tabulated cross sections (ioffe data) are not part of the reference."""
+    if "Ruth" not in elastic:
+        raise NotImplementedError("elastic %r: Mott tables (ioffe data) are not available" % elastic)
+    if dispatch == "intended":
+        if elastic not in _lib.ELASTIC:
+            raise ValueError("unknown elastic model %r" % elastic)
+        return _lib.ELASTIC[elastic]
+    if mode == _lib.MODE_DS:
+        if elastic == "Ruth_vanilla":
+            return _lib.ELASTIC_RUTH
+        if "vanilla_wDefl" in elastic:
+            raise NameError("name 'ruther_sigma_wDefl' is not defined")
+        if elastic == "Ruth_nigram":
+            return _lib.ELASTIC_NIGRAM
+        if "nigram_wDefl" in elastic:
+            return _lib.ELASTIC_NIGRAM_WDEFL
+    else:
+        if "vanilla" in elastic:
+            return _lib.ELASTIC_RUTH
+        if "nigram" in elastic:
+            return _lib.ELASTIC_NIGRAM
+    raise ValueError("elastic %r selects no elastic cross section" % elastic)
+
+
 def make_sim(input_par, num_el, seed=0, first_electron=0, precision=_lib.FP32, sim_id=0,
              hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
-             tally_flags=0, J_scale=1.0, n_scale=1.0):
+             tally_flags=0, J_scale=1.0, n_scale=1.0, elastic_dispatch="reference"):
     p = with_defaults(input_par)
     s = _lib.Sim()
     s.mode = mode_of(p)
@@ -56,10 +94,14 @@ def make_sim(input_par, num_el, seed=0, first_electron=0, precision=_lib.FP32, s
     s.hist_T_bins, s.hist_T_width = int(hist_T[0]), float(hist_T[1])
     s.J_scale = float(J_scale)
     s.n_scale = float(n_scale)
-    if p.get("elastic", "Ruth_vanilla") != "Ruth_vanilla":
-        raise NotImplementedError("elastic model %r: only Ruth_vanilla is on the GPU path" % p["elastic"])
-    if p.get("diffMFP"):
-        raise NotImplementedError("diffMFP: the diffraction channel is not on the GPU path")
+    s.elastic = elastic_model(p.get("elastic", "Ruth_vanilla"), s.mode, elastic_dispatch)
+    s.diff_mfp = 0
+    if p.get("diffMFP") and s.mode == _lib.MODE_DS:
+        # the channel reads the material's extinction distance
+        # (MC/tools/material.py:225-226 defines it for Si only)
+        if not _lib.material(p["material"]).xip_g > 0:
+            raise KeyError("xip_g")
+        s.diff_mfp = 1
     return s
 
 

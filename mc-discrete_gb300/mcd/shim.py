@@ -45,6 +45,7 @@ def _type_names(mat, mode, elastic):
     names = ["Ruth", "Moller", "Quinn"]
     for k in range(mat.n_shells):
         names.append("Gryz" + mat.shell_name[k].value.decode())
+    names += [""] * (_lib.CH_DIFF - len(names)) + ["diff"]
     return names
 
 

@@ -21,7 +21,7 @@ class Mat(C.Structure):
     _fields_ = [("Z", C.c_double), ("n_val", C.c_double), ("E_val", C.c_double), ("atnd", C.c_double),
                 ("plasmon_e", C.c_double), ("fermi_e", C.c_double), ("J", C.c_double), ("bethe_k", C.c_double),
                 ("n_shells", C.c_int), ("shell_E", C.c_double * MAX_SHELLS),
-                ("shell_n", C.c_double * MAX_SHELLS)]
+                ("shell_n", C.c_double * MAX_SHELLS), ("xip_g", C.c_double)]
 
 
 class Tab(C.Structure):
@@ -32,7 +32,8 @@ class Sim(C.Structure):
     _fields_ = [("mode", C.c_int), ("bethe", C.c_int), ("E0", C.c_double), ("Emin", C.c_double),
                 ("tilt", C.c_double), ("Wc", C.c_double), ("thickness", C.c_double),
                 ("max_scatt", C.c_longlong), ("seed", C.c_ulonglong), ("sim_id", C.c_uint),
-                ("quirks", C.c_uint), ("J_scale", C.c_double), ("n_scale", C.c_double)]
+                ("quirks", C.c_uint), ("J_scale", C.c_double), ("n_scale", C.c_double),
+                ("elastic", C.c_int), ("diff", C.c_int)]
 
 
 class Out(C.Structure):
@@ -75,6 +76,7 @@ def mat_struct(mat):
     for k, (_, Es, ns) in enumerate(mat.shells):
         m.shell_E[k] = Es
         m.shell_n[k] = ns
+    m.xip_g = mat.xip_g or 0.0
     return m
 
 
@@ -95,14 +97,17 @@ class HostTable:
 
 
 BETHE = {"classical": 0, "JL": 1, "explicit": 2}
+ELASTIC = list(O.ELASTIC_MODELS)
 
 
 def run(mat, E0, Emin, tilt, n, seed=0, first=0, mode="DS", Wc=100.0, tables=None, bethe="classical",
-        thickness=1e30, max_scatt=10 ** 15, sim_id=0, quirks=7, J_scale=1.0, n_scale=1.0, nthreads=None):
-    """Run n electrons; returns a dict of per-electron arrays + channel counts."""
+        thickness=1e30, max_scatt=10 ** 15, sim_id=0, quirks=7, J_scale=1.0, n_scale=1.0, nthreads=None,
+        elastic="Ruth_vanilla", diff=False):
+    """Run n electrons; returns a dict of per-electron arrays + channel counts.
+    elastic is a resolved model name (mcd_oracle.ELASTIC_MODELS)."""
     L = lib()
     s = Sim(0 if mode == "DS" else 1, BETHE[bethe], E0, Emin, tilt, Wc, thickness, max_scatt, seed, sim_id,
-            quirks, J_scale, n_scale)
+            quirks, J_scale, n_scale, ELASTIC.index(elastic), 1 if diff else 0)
     m = mat_struct(mat)
     res = dict(outcome=np.zeros(n, np.uint8), flags=np.zeros(n, np.uint8), final_E=np.zeros(n),
                dir=np.zeros((n, 3)), last_pos=np.zeros((n, 3)), max_z=np.zeros(n),

@@ -34,6 +34,7 @@ typedef struct {
     double Z, n_val, E_val, atnd, plasmon_e, fermi_e, J, bethe_k;
     int n_shells;
     double shell_E[MCO_MAX_SHELLS], shell_n[MCO_MAX_SHELLS];
+    double xip_g;      /* extinction distance of the diffraction channel (0: none) */
 } mco_mat;
 
 typedef struct {
@@ -52,6 +53,8 @@ typedef struct {
     unsigned sim_id;
     unsigned quirks;   /* bit0 crossing step, bit1 half-phi fold, bit2 NaN */
     double J_scale, n_scale;
+    int elastic;       /* 0 Ruth_vanilla, 1 _vanilla_wDefl, 2 _nigram, 3 _nigram_wDefl */
+    int diff;          /* diffMFP: the diffraction channel (DS)             */
 } mco_sim;
 
 typedef struct {
@@ -66,8 +69,8 @@ typedef struct {
     unsigned long long* nan_events;
 } mco_out;
 
-enum { OUT_NONE = 0, OUT_BKS = 1, OUT_ABS = 2, OUT_TRSM = 3, OUT_LONG = 5 };
-enum { CH_RUTH = 0, CH_MOLLER = 1, CH_QUINN = 2, CH_GRYZ0 = 3 };
+enum { OUT_NONE = 0, OUT_BKS = 1, OUT_ABS = 2, OUT_TRSM = 3, OUT_TRDF = 4, OUT_LONG = 5 };
+enum { CH_RUTH = 0, CH_MOLLER = 1, CH_QUINN = 2, CH_GRYZ0 = 3, CH_DIFF = 11 };
 
 /* ---------------- Philox4x32-10 ---------------- */
 static void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
@@ -97,6 +100,33 @@ static double ruther_sigma(double E, double Z) {
     double r = (Ek + 511.0) / (Ek + 1024.0);
     return 5.21e-21 * (Z * Z / (Ek * Ek)) * (r * r) * (4.0 * PI_D) / (a * (1.0 + a));
 }
+
+/* crossSections.py:63-86 */
+static double ruther_sigma_wdefl(double E, double Z) {
+    double a = alpha_(E, Z);
+    double Ek = E * 1e-3;
+    double r = (Ek + 511.0) / (Ek + 1024.0);
+    return 5.21e-21 * (Z * (Z + 1.0) / (Ek * Ek)) * (r * r) * (4.0 * PI_D) / (a * (1.0 + a));
+}
+
+/* crossSections.py:90-147, Nigram screening 0.48 * 5.43 Z^(2/3) / E */
+static double ruther_n_sigma(double E, double Z, int wdefl) {
+    double b = 0.48 * (5.43 * pow(Z, 2.0 / 3.0) / E);
+    double zz = wdefl ? (Z + 1.0) * Z : Z * Z;
+    return PI_EFOUR * zz / (4.0 * b * (1.0 + b) * (E * E));
+}
+
+static double elastic_sigma(int model, double E, double Z) {
+    switch (model) {
+        case 1: return ruther_sigma_wdefl(E, Z);
+        case 2: return ruther_n_sigma(E, Z, 0);
+        case 3: return ruther_n_sigma(E, Z, 1);
+        default: return ruther_sigma(E, Z);
+    }
+}
+
+/* crossSections.py:329-349 */
+static double diffr_sigma(double xip_g, double n) { return 1.0 / (n * xip_g) * 1e13; }
 
 static double moller_sigma(double E, double Wc, double nfree) {
     if (E <= Wc) return 0.0;
@@ -163,6 +193,7 @@ typedef struct {
     double max_z;
     long long steps;
     unsigned nan_events;
+    int diffracting;
 } el_t;
 
 static void save_row(el_t* e, int oc) {
@@ -181,7 +212,7 @@ static void update_xyz(el_t* e, double s, double maxz) {
     if (p[2] <= 0.0) {
         save_row(e, OUT_BKS);
     } else if (p[2] >= maxz) {
-        save_row(e, OUT_TRSM);
+        save_row(e, e->diffracting ? OUT_TRDF : OUT_TRSM);
     } else {
         memcpy(e->pos, p, sizeof p);
         if (p[2] > e->max_z) e->max_z = p[2];
@@ -265,16 +296,17 @@ static void run_one(job_t* j, long long i) {
         double W, c2, hphi, sl;
         int ch;
         if (s->mode == 0) {
-            double sig[3 + MCO_MAX_SHELLS];
-            int code[3 + MCO_MAX_SHELLS];
+            double sig[4 + MCO_MAX_SHELLS];
+            int code[4 + MCO_MAX_SHELLS];
             int nch = 0;
-            sig[nch] = ruther_sigma(Ei, m->Z); code[nch++] = CH_RUTH;
+            sig[nch] = elastic_sigma(s->elastic, Ei, m->Z); code[nch++] = CH_RUTH;
             sig[nch] = moller_sigma(Ei, s->Wc, m->n_val); code[nch++] = CH_MOLLER;
             for (int k = 0; k < m->n_shells; ++k) {
                 sig[nch] = gryz_sigma(Ei, m->shell_E[k], m->shell_n[k]);
                 code[nch++] = CH_GRYZ0 + k;
             }
             sig[nch] = quinn_sigma(Ei, m->plasmon_e, m->fermi_e, n_at); code[nch++] = CH_QUINN;
+            if (s->diff) { sig[nch] = diffr_sigma(m->xip_g, n_at); code[nch++] = CH_DIFF; }
             double tot = 0.0;
             for (int k = 0; k < nch; ++k) tot += sig[k];
             double mfp = mfp_from_sigma(tot, n_at);
@@ -285,9 +317,14 @@ static void run_one(job_t* j, long long i) {
                 cum += sig[k];
                 if (cum / tot >= U) { ch = code[k]; break; }
             }
+            if (ch == CH_DIFF) mfp = m->xip_g;
+            e.diffracting = ch == CH_DIFF;
             sl = -mfp * log(unit(c[1]));
             update_xyz(&e, sl, maxz);
-            if (ch == CH_RUTH) {
+            if (ch == CH_DIFF) {
+                W = 0.0;
+                c2 = 1.0;
+            } else if (ch == CH_RUTH) {
                 W = 0.0;
                 double a = alpha_(Ei, m->Z), u = unit(c[2]);
                 c2 = 1.0 - (a * u / (1.0 + a - u));
@@ -305,7 +342,7 @@ static void run_one(job_t* j, long long i) {
             }
         } else {
             ch = CH_RUTH;
-            double mfp = mfp_from_sigma(ruther_sigma(Ei, m->Z), n_at);
+            double mfp = mfp_from_sigma(elastic_sigma(s->elastic, Ei, m->Z), n_at);
             sl = -mfp * log(unit(c[1]));
             update_xyz(&e, sl, maxz);
             W = sl * stopping(s, m, Ei, n_at, J);
@@ -340,6 +377,7 @@ int mco_run(const mco_sim* s, const mco_mat* m, const mco_table* tm, const mco_t
             unsigned long long first, long long n, mco_out* out, int nthreads) {
     if (!s || !m || !out || n < 0) return 1;
     if (s->mode == 0 && (!tm || !tg)) return 1;
+    if (s->mode == 0 && s->diff && !(m->xip_g > 0)) return 1;
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     job_t* jobs = (job_t*)calloc((size_t)nthreads, sizeof(job_t));

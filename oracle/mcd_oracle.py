@@ -59,7 +59,7 @@ SPECIES = {
                bethe_k=0.815, name_val="3s2-3p1",
                shells=[("1s", 1559.0, 2), ("2s", 118.0, 2), ("2p", 73.5, 6)]),
     "Si": dict(Z=14, n_val=4, E_val=99.42, density=2.33, atwt=28.085,
-               bethe_k=0.822, name_val="3s2-3p2",
+               bethe_k=0.822, name_val="3s2-3p2", xip_g=1360.0,
                shells=[("1s", 1189.0, 2), ("2s", 149.0, 2), ("2p", 100.0, 6)]),
     "Cu": dict(Z=29, n_val=11, E_val=75.1, density=8.96, atwt=63.546,
                bethe_k=0.83, name_val="3d10-4s2",
@@ -88,6 +88,8 @@ class Material:
         self.bethe_k = p["bethe_k"]
         self.name_val = p["name_val"]
         self.shells = list(p["shells"])
+        # extinction distance of the diffraction channel (material.py:225-226, Si only)
+        self.xip_g = p.get("xip_g")
         # atomic number density in m^-3 (material.py:15-31)
         self.atnd = p["density"] * AVOGADRO / p["atwt"] * 1e6
         nv = self.n_val * self.atnd
@@ -121,6 +123,53 @@ def ruther_sigma(E, Z):
     # r*r, not r**2: glibc's pow(x, 2) is not always correctly rounded, and
     # the C oracle's compiler folds pow(r, 2) to r*r
     return 5.21e-21 * (Z * Z / (Ek * Ek)) * (r * r) * (4.0 * PI) / (a * (1.0 + a))
+
+
+def ruther_sigma_wDefl(E, Z):
+    """crossSections.py:63-86: ruther_sigma with Z^2 -> Z (Z + 1)."""
+    a = alpha(E, Z)
+    Ek = E * 1e-3
+    r = (Ek + 511.0) / (Ek + 1024.0)
+    return 5.21e-21 * (Z * (Z + 1) / (Ek * Ek)) * (r * r) * (4.0 * PI) / (a * (1.0 + a))
+
+
+def _nigram_beta(E, Z):
+    """crossSections.py:108-112: 0.48 * 5.43 Z^(2/3) / E."""
+    return 0.48 * (5.43 * Z ** (2.0 / 3.0) / E)
+
+
+def ruther_N_sigma(E, Z):
+    """crossSections.py:90-116 (Nigram screening), cm^2."""
+    b = _nigram_beta(E, Z)
+    return PI_EFOUR * (Z * Z) / (4.0 * b * (1.0 + b) * (E * E))
+
+
+def ruther_N_sigma_wDefl(E, Z):
+    """crossSections.py:120-147: ruther_N_sigma with Z^2 -> Z (Z + 1)."""
+    b = _nigram_beta(E, Z)
+    return PI_EFOUR * ((Z + 1) * Z) / (4.0 * b * (1.0 + b) * (E * E))
+
+
+ELASTIC_MODELS = ("Ruth_vanilla", "Ruth_vanilla_wDefl", "Ruth_nigram", "Ruth_nigram_wDefl")
+
+
+def elastic_sigma(model, E, Z):
+    """The elastic total cross section of a resolved model name (the
+    reference's string dispatch is resolved by the caller)."""
+    if model == "Ruth_vanilla":
+        return ruther_sigma(E, Z)
+    if model == "Ruth_vanilla_wDefl":
+        return ruther_sigma_wDefl(E, Z)
+    if model == "Ruth_nigram":
+        return ruther_N_sigma(E, Z)
+    if model == "Ruth_nigram_wDefl":
+        return ruther_N_sigma_wDefl(E, Z)
+    raise ValueError(model)
+
+
+def diffr_sigma(xip_g, n):
+    """crossSections.py:329-349: 1 / (n xip_g) in units m^3/nm/cm^2 = 1e13, cm^2."""
+    return 1.0 / (n * xip_g) * 1e13
 
 
 def moller_sigma(E, Wc, nfree):
@@ -398,18 +447,20 @@ class Electron:
         self.steps = 0
         self.max_z = 0.0
         self.nan_events = 0
+        self.diffracting = False
 
     def save(self):
         self.rows.append((self.outcome, self.E, list(self.dir), list(self.pos)))
 
     def update_xyz(self, s, maxz):
-        """electron.py:64-84 (the diffraction flag is never set on this path)."""
+        """electron.py:64-84: leaving through the bottom face right after a
+        diffraction event is 'trdf', otherwise 'trsm'."""
         p = [self.pos[i] + s * self.dir[i] for i in range(3)]
         if p[2] <= 0.0:
             self.outcome = "bks"
             self.save()
         elif p[2] >= maxz:
-            self.outcome = "trsm"
+            self.outcome = "trdf" if self.diffracting else "trsm"
             self.save()
         else:
             self.pos = p
@@ -428,21 +479,26 @@ class Electron:
         self.dir, self.y = _rotate(c2, half_phi, self.dir, self.y)
 
 
-CH_RUTH, CH_MOLLER, CH_QUINN, CH_GRYZ0 = 0, 1, 2, 3
+CH_RUTH, CH_MOLLER, CH_QUINN, CH_GRYZ0, CH_DIFF = 0, 1, 2, 3, 11
 
 
 def channel_names(mat):
-    """Channel codes -> reference type labels (scattering.py:483-508)."""
-    return ["Ruth", "Moller", "Quinn"] + ["Gryz" + s[0] for s in mat.shells]
+    """Channel codes -> reference type labels (scattering.py:483-516)."""
+    names = ["Ruth", "Moller", "Quinn"] + ["Gryz" + s[0] for s in mat.shells]
+    names += [""] * (CH_DIFF - len(names)) + ["diff"]
+    return names
 
 
-def ds_sigmas(E, mat, Wc):
-    """scattering.py:483-508 in the reference's insertion order, as
-    (code, sigma) pairs: Ruth, Moller, Gryz<shell> in name_s order, Quinn."""
-    out = [(CH_RUTH, ruther_sigma(E, mat.Z)), (CH_MOLLER, moller_sigma(E, Wc, mat.n_val))]
+def ds_sigmas(E, mat, Wc, elastic="Ruth_vanilla", diff=False):
+    """scattering.py:483-516 in the reference's insertion order, as
+    (code, sigma) pairs: Ruth, Moller, Gryz<shell> in name_s order, Quinn,
+    then the diffraction channel when diffMFP is on."""
+    out = [(CH_RUTH, elastic_sigma(elastic, E, mat.Z)), (CH_MOLLER, moller_sigma(E, Wc, mat.n_val))]
     for k, (_, Es, ns) in enumerate(mat.shells):
         out.append((CH_GRYZ0 + k, gryz_sigma(E, Es, ns)))
     out.append((CH_QUINN, quinn_sigma(E, mat.plasmon_e, mat.fermi_e, mat.atnd)))
+    if diff:
+        out.append((CH_DIFF, diffr_sigma(mat.xip_g, mat.atnd)))
     return out
 
 
@@ -462,15 +518,18 @@ def pick_channel(sig, U, sort_channels):
     return sig[min(i, len(sig) - 1)][0]
 
 
-def trajectory_ds(el, mat, Wc, maxScatt, maxz, tables, rng):
+def trajectory_ds(el, mat, Wc, maxScatt, maxz, tables, rng, elastic="Ruth_vanilla", diff=False):
     """singleScatter.py:10-41 with scatter_discrete (scattering.py:440-679).
 
-    tables = (moller Table, gryz Table for the outermost shell)."""
+    tables = (moller Table, gryz Table for the outermost shell).  With diff
+    (diffMFP) a diffraction event steps with mean free path xip_g
+    (scattering.py:540-548), loses nothing and keeps its direction
+    (:658-668), and marks the electron diffracting for the exit test."""
     t_m, t_g = tables
     num = 0
     while el.outcome not in ("abs", "bks", "trsm", "trdf", "long"):
         Ei = el.E
-        sig = ds_sigmas(Ei, mat, Wc)
+        sig = ds_sigmas(Ei, mat, Wc, elastic, diff)
         stot = 0.0
         for _, s in sig:
             stot += s
@@ -483,9 +542,15 @@ def trajectory_ds(el, mat, Wc, maxScatt, maxz, tables, rng):
             return
         rng.begin_event(num - 1)
         ch = pick_channel(sig, rng.u(0), rng.sort_channels)
+        if ch == CH_DIFF:
+            mfp = mat.xip_g
+        el.diffracting = ch == CH_DIFF
         s = -mfp * math.log(rng.u(1))
         el.update_xyz(s, maxz)
-        if ch == CH_RUTH:
+        if ch == CH_DIFF:
+            W = 0.0
+            c2 = 1.0
+        elif ch == CH_RUTH:
             W = 0.0
             c2 = rutherford_c2(Ei, mat.Z, rng.u(2))
         elif ch == CH_MOLLER:
@@ -527,7 +592,7 @@ class ContStatus:
         self.clamped = 0        # dE >= E (scattering.py:822 asserts)
 
 
-def trajectory_cont(el, mat, maxScatt, maxz, model, rng, status=None, J=None, n=None):
+def trajectory_cont(el, mat, maxScatt, maxz, model, rng, status=None, J=None, n=None, elastic="Ruth_vanilla"):
     """singleScatter.py:205-239 with scatter_continuous_* (scattering.py:753-883).
 
     maxz is passed (the reference's caller omits it); an energy loss >= E is
@@ -536,7 +601,7 @@ def trajectory_cont(el, mat, maxScatt, maxz, model, rng, status=None, J=None, n=
     num = 0
     while el.outcome not in ("abs", "bks", "trsm"):
         Ei = el.E
-        mfp = mfp_from_sigma(ruther_sigma(Ei, mat.Z), n_at)
+        mfp = mfp_from_sigma(elastic_sigma(elastic, Ei, mat.Z), n_at)
         pos0 = list(el.pos)
         num += 1
         if num > maxScatt:
@@ -563,23 +628,23 @@ def trajectory_cont(el, mat, maxScatt, maxz, model, rng, status=None, J=None, n=
 
 
 def run_ds(mat, E0, Emin, s_tilt, Wc, maxScatt, maxz, tables, n_el, seed, sim=0,
-           first=0, record=False):
+           first=0, record=False, elastic="Ruth_vanilla", diff=False):
     """One DS simulation on the Philox stream; returns the Electron objects."""
     d0 = beam_direction(s_tilt)
     out = []
     for k in range(first, first + n_el):
         el = Electron(E0, Emin, d0, record)
-        trajectory_ds(el, mat, Wc, maxScatt, maxz, tables, PhiloxStream(seed, k, sim))
+        trajectory_ds(el, mat, Wc, maxScatt, maxz, tables, PhiloxStream(seed, k, sim), elastic, diff)
         out.append(el)
     return out
 
 
 def run_cont(mat, E0, Emin, s_tilt, maxScatt, maxz, model, n_el, seed, sim=0, first=0,
-             record=False, J=None, n=None, status=None):
+             record=False, J=None, n=None, status=None, elastic="Ruth_vanilla"):
     d0 = beam_direction(s_tilt)
     out = []
     for k in range(first, first + n_el):
         el = Electron(E0, Emin, d0, record)
-        trajectory_cont(el, mat, maxScatt, maxz, model, PhiloxStream(seed, k, sim), status, J, n)
+        trajectory_cont(el, mat, maxScatt, maxz, model, PhiloxStream(seed, k, sim), status, J, n, elastic)
         out.append(el)
     return out

@@ -18,9 +18,13 @@ GOLDEN_TABLES = {
 }
 
 
-def input_par(species, E0, Emin, tilt, Wc=100.0, tol=1e-3, mode="DS", bethe="classical"):
+def input_par(species, E0, Emin, tilt, Wc=100.0, tol=1e-3, mode="DS", bethe="classical", elastic="Ruth_vanilla",
+              diffMFP=False, thickness=1e30):
     return dict(material=species, E0=E0, Emin=Emin, s_tilt=tilt, Wc=Wc, tol_E=tol, tol_W=tol, mode=mode,
-                Bethe_model=bethe, num_el=0)
+                Bethe_model=bethe, num_el=0, elastic=elastic, diffMFP=diffMFP, thickness=thickness)
+
+
+ELASTIC_NAME = {v: k for k, v in _lib.ELASTIC.items()}
 
 
 def gpu_tables(p):
@@ -41,8 +45,10 @@ def run_pair(p, n, seed=1, precision="fp64", nthreads=None):
     mat = O.Material(p["material"])
     ds = "DS" in p["mode"]
     ht = host_copies(gpu_tables(p)) if ds else None
+    sim = engine.make_sim(p, n)
     c = coracle.run(mat, p["E0"], p["Emin"], p["s_tilt"], n, seed=seed, mode="DS" if ds else "cont",
-                    Wc=p["Wc"], tables=ht, bethe=p.get("Bethe_model", "classical"), nthreads=nthreads)
+                    Wc=p["Wc"], tables=ht, bethe=p.get("Bethe_model", "classical"), nthreads=nthreads,
+                    elastic=ELASTIC_NAME[sim.elastic], diff=bool(sim.diff_mfp), thickness=sim.thickness)
     return g, c
 
 

@@ -81,6 +81,12 @@ def part_physics():
         out[spc + "/const"] = np.array([mat.atnd, mat.plasmon_e, mat.fermi_e])
         out[spc + "/alpha"] = np.array([cs.alpha(E, p["Z"]) for E in Egrid])
         out[spc + "/ruth"] = np.array([cs.ruther_sigma(E, p["Z"]) for E in Egrid])
+        out[spc + "/ruth_wdefl"] = np.array([cs.ruther_sigma_wDefl(E, p["Z"]) for E in Egrid])
+        out[spc + "/ruth_nigram"] = np.array([cs.ruther_N_sigma(E, p["Z"]) for E in Egrid])
+        out[spc + "/ruth_nigram_wdefl"] = np.array([cs.ruther_N_sigma_wDefl(E, p["Z"]) for E in Egrid])
+        if "xip_g" in p:
+            out[spc + "/xip_g"] = np.array(float(p["xip_g"]))
+            out[spc + "/diffr"] = np.array(cs.diffr_sigma(p["xip_g"], mat.atnd, 0.0))
         for Wc in (10.0, 50.0, 100.0):
             out[spc + "/moller/%g" % Wc] = np.array([cs.moller_sigma(E, Wc, p["n_val"]) for E in Egrid])
         for sh in p["name_s"]:
@@ -193,17 +199,27 @@ SCAT_COLS = ["type", "E", "E_loss", "pol_angle", "az_angle", "pathl", "position"
 EL_COLS = ["outcome", "final_E", "final_dir", "last_pos"]
 
 
-def run_ref_ds(mat, tables, E0, Emin, tilt, Wc, seed, maxz=INF_Z, scat_cols=SCAT_COLS):
+def run_ref_ds(mat, tables, E0, Emin, tilt, Wc, seed, maxz=INF_Z, scat_cols=SCAT_COLS, elastic="Ruth_vanilla",
+               diffMFP=False):
+    """One reference DS trajectory.  With diffMFP the discrete scatter class
+    gets the extinction distance as a class attribute: its constructor reads
+    self.xip_g, whose assignment is commented out (MC/tools/scattering.py:458),
+    so without it the reference cannot run that path at all."""
     m = _load()
+    sd = m["scattering"].scatter_discrete
+    if diffMFP:
+        sd.xip_g = mat.params["xip_g"]
+    elif hasattr(sd, "xip_g"):
+        del sd.xip_g
     d0 = np.array([-np.sin(np.radians(tilt)), 0.0, np.cos(np.radians(tilt))])
     el = m["electron"].electron(E0, Emin, np.array([0.0, 0.0, 0.0]), d0,
                                 {"el_output": EL_COLS, "scat_output": scat_cols})
     random.seed(seed)
-    m["singleScatter"].trajectory_DS(el, mat, Wc, BIG_MAXSCATT, maxz, "Ruth_vanilla", tables, False)
+    m["singleScatter"].trajectory_DS(el, mat, Wc, BIG_MAXSCATT, maxz, elastic, tables, diffMFP)
     return el.el_output.dict, el.scat_output.dict
 
 
-def run_ref_cont(mat, E0, Emin, tilt, seed, maxz=INF_Z):
+def run_ref_cont(mat, E0, Emin, tilt, seed, maxz=INF_Z, elastic="Ruth_vanilla"):
     """The loop of trajectory_cont_cl (MC/tools/singleScatter.py:205-239) with
     maxz passed, on the reference's classical scatter class and electron."""
     m = _load()
@@ -213,7 +229,7 @@ def run_ref_cont(mat, E0, Emin, tilt, seed, maxz=INF_Z):
                                  "scat_output": ["type", "E_loss", "pol_angle", "az_angle", "pathl", "energy"]})
     random.seed(seed)
     while (el.outcome != "abs") and (el.outcome != "bks") and (el.outcome != "trsm"):
-        sc = m["scattering"].scatter_continuous_classical(el, mat, "Ruth_vanilla", None)
+        sc = m["scattering"].scatter_continuous_classical(el, mat, elastic, None)
         sc.compute_pathl()
         el.update_xyz(sc.pathl, maxz)
         sc.compute_Eloss()
@@ -259,42 +275,55 @@ def _flatten(el_list, sc_list, types):
 
 
 def type_labels(mat_params):
-    return ["Ruth", "Moller", "Quinn"] + ["Gryz" + s for s in mat_params["name_s"]]
+    return ["Ruth", "Moller", "Quinn"] + ["Gryz" + s for s in mat_params["name_s"]] + ["diff"]
 
 
 def part_replay():
     out = {}
-    # DS: cfg1 physics (Si 10 keV) and cfg3 physics (Au 30 keV, tilt 70)
-    for tag, cfg, tilt, n, base in (("ds_si", CFG1, 0.0, 24, 1000), ("ds_au", CFG3, 70.0, 3, 2000)):
+    # DS: cfg1 physics (Si 10 keV) and cfg3 physics (Au 30 keV, tilt 70); the
+    # Nigram elastic cross sections; the diffraction channel in a Si film
+    # (elastic model, diffMFP, thickness in A)
+    for tag, cfg, tilt, n, base, elastic, diff, maxz in (
+            ("ds_si", CFG1, 0.0, 24, 1000, "Ruth_vanilla", False, INF_Z),
+            ("ds_au", CFG3, 70.0, 3, 2000, "Ruth_vanilla", False, INF_Z),
+            ("ds_si_nigram", CFG1, 0.0, 8, 5000, "Ruth_nigram", False, INF_Z),
+            ("ds_si_nigram_wdefl", CFG1, 0.0, 8, 6000, "Ruth_nigram_wDefl", False, INF_Z),
+            ("ds_si_diff", CFG1, 0.0, 24, 7000, "Ruth_vanilla", True, 3000.0)):
         tables, mat = ds_tables(cfg)
         _, spc, E0, Emin, Wc, tol = cfg
         types = type_labels(mat.params)
         els, scs = [], []
         for k in range(n):
             with np.errstate(invalid="ignore"):
-                e, s = run_ref_ds(mat, tables, E0, Emin, tilt, Wc, base + k)
+                e, s = run_ref_ds(mat, tables, E0, Emin, tilt, Wc, base + k, maxz=maxz, elastic=elastic,
+                                  diffMFP=diff)
             els.append(e)
             scs.append(s)
         flat = _flatten(els, scs, types)
         for k, v in flat.items():
             out[tag + "/" + k] = v
+        out[tag + "/elastic"] = np.array(elastic)
+        out[tag + "/diffMFP"] = np.array(diff)
+        out[tag + "/thickness"] = np.array(maxz)
         out[tag + "/cfg"] = np.array([E0, Emin, tilt, Wc, tol])
         out[tag + "/species"] = np.array(spc)
         out[tag + "/seeds"] = np.arange(base, base + n)
         print(tag, "events", flat["ev_off"][-1], "rows", flat["row_off"][-1], flush=True)
     # continuous, classical Bethe: Al 15 keV tilt 70 (cfg5 physics), Cu 20 keV tilt 70
     m = _load()
-    for tag, spc, E0, tilt, n, base in (("cont_al", "Al", 15000.0, 70.0, 8, 3000),
-                                        ("cont_cu", "Cu", 20000.0, 70.0, 4, 4000)):
+    for tag, spc, E0, tilt, n, base, elastic in (("cont_al", "Al", 15000.0, 70.0, 8, 3000, "Ruth_vanilla"),
+                                                 ("cont_cu", "Cu", 20000.0, 70.0, 4, 4000, "Ruth_vanilla"),
+                                                 ("cont_al_nigram", "Al", 15000.0, 70.0, 4, 8000, "Ruth_nigram")):
         mat = m["material"].material(spc)
         els, scs = [], []
         for k in range(n):
-            e, s = run_ref_cont(mat, E0, 1000.0, tilt, base + k)
+            e, s = run_ref_cont(mat, E0, 1000.0, tilt, base + k, elastic=elastic)
             els.append(e)
             scs.append(s)
-        flat = _flatten(els, scs, ["Ruth_vanilla"])
+        flat = _flatten(els, scs, [elastic])
         for k, v in flat.items():
             out[tag + "/" + k] = v
+        out[tag + "/elastic"] = np.array(elastic)
         out[tag + "/cfg"] = np.array([E0, 1000.0, tilt])
         out[tag + "/species"] = np.array(spc)
         out[tag + "/seeds"] = np.arange(base, base + n)

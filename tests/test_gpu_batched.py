@@ -21,6 +21,8 @@ SIMS = [
     dict(input_par("Al", 30000.0, 1000.0, 20.0), num_el=1200),
     dict(input_par("Cu", 20000.0, 1000.0, 70.0, mode="cont", bethe="JL"), num_el=2500),
     dict(input_par("Al", 15000.0, 1000.0, 70.0, mode="cont", bethe="classical"), num_el=64),
+    dict(input_par("Si", 10000.0, 1000.0, 0.0, elastic="Ruth_nigram"), num_el=1500),
+    dict(input_par("Si", 10000.0, 1000.0, 0.0, diffMFP=True, thickness=3000.0), num_el=2000),
 ]
 
 INT_KEYS = ("none", "bks", "abs", "trsm", "trdf", "long", "events", "double_rows", "nan_events",
@@ -58,7 +60,7 @@ def test_batched_equals_plain(plain_tallies, refill, block, variant):
         assert np.array_equal(t["hist_E"], ref["hist_E"])
         assert np.array_equal(t["hist_T"], ref["hist_T"])
         assert abs(t["sum_E_bks"] - ref["sum_E_bks"]) <= 1e-9 * max(1.0, ref["sum_E_bks"])
-        assert sum(t[o] for o in ("bks", "abs", "trsm", "long")) == SIMS[k]["num_el"]
+        assert sum(t[o] for o in ("bks", "abs", "trsm", "trdf", "long")) == SIMS[k]["num_el"]
 
 
 @pytest.mark.parametrize("variant", [0, 1])
@@ -71,8 +73,8 @@ def test_tabulated_cross_sections_follow_inline(variant):
     changed = 0
     for k, (t, r) in enumerate(zip(tab, inl)):
         n = sims[k]["num_el"]
-        assert sum(t[o] for o in ("bks", "abs", "trsm", "long")) == n
-        for o in ("bks", "abs", "trsm"):
+        assert sum(t[o] for o in ("bks", "abs", "trsm", "trdf", "long")) == n
+        for o in ("bks", "abs", "trsm", "trdf"):
             assert abs(t[o] - r[o]) <= 3 + 1e-3 * n, (k, o, t[o], r[o])
         assert abs(t["events"] - r["events"]) <= 1e-3 * r["events"], k
         assert np.abs(t["hist_E"].astype(np.int64) - r["hist_E"]).sum() <= 6 + 2e-3 * n, k

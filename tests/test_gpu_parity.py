@@ -23,6 +23,12 @@ CASES = [
     ("al15_cont_cl", input_par("Al", 15000.0, 1000.0, 70.0, mode="cont", bethe="classical"), 3000),
     ("cu20_cont_jl", input_par("Cu", 20000.0, 1000.0, 70.0, mode="cont", bethe="JL"), 2000),
     ("si10_cont_ex", input_par("Si", 10000.0, 1000.0, 0.0, mode="cont", bethe="explicit"), 2000),
+    # elastic models (MC/tools/crossSections.py:63-147) and the diffraction
+    # channel in a 3000 A Si film (diffMFP, 'trdf' exits)
+    ("si10_ds_nigram", input_par("Si", 10000.0, 1000.0, 0.0, elastic="Ruth_nigram"), 2000),
+    ("cu20_ds_nigram_wdefl", input_par("Cu", 20000.0, 1000.0, 45.0, elastic="Ruth_nigram_wDefl"), 400),
+    ("si_film_diff", input_par("Si", 10000.0, 1000.0, 0.0, diffMFP=True, thickness=3000.0), 3000),
+    ("al15_cont_nigram", input_par("Al", 15000.0, 1000.0, 70.0, mode="cont", elastic="Ruth_nigram"), 2000),
 ]
 
 
@@ -43,7 +49,10 @@ def test_fp64_follows_oracle_trajectories(name, p, n):
     t = g.tally
     assert t["bks"] == int((e["outcome"] == 1).sum())
     assert t["events"] == int(e["n_events"].sum())
-    assert t["bks"] + t["abs"] + t["trsm"] + t["long"] == n
+    assert t["bks"] + t["abs"] + t["trsm"] + t["trdf"] + t["long"] == n
+    if p.get("diffMFP"):
+        assert t["trdf"] == int((e["outcome"] == 4).sum()) > 0
+        assert abs(t["trdf"] - int((c["outcome"] == 4).sum())) <= 0.01 * n
 
 
 @pytest.mark.parametrize("name,p,n", CASES, ids=[c[0] for c in CASES])

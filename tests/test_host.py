@@ -39,7 +39,7 @@ def test_struct_layouts_match():
 
 def test_abi_and_errors():
     L = _lib.lib()
-    assert L.mcd_abi_version() == _lib.ABI_VERSION == 2
+    assert L.mcd_abi_version() == _lib.ABI_VERSION == 3
     assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
     m = _lib.Material()
     assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
@@ -125,6 +125,41 @@ def test_input_parser(tmp_path):
     assert p["thickness"] == 5e5 and p["maxScatt"] == 100000
     q = config.with_defaults({"E0": 1.0})
     assert q["E0"] == 1.0 and q["thickness"] == 1e30
+
+
+def test_elastic_dispatch_follows_reference_string_tests():
+    from mcd import engine
+    DS, CONT = _lib.MODE_DS, _lib.MODE_CONT
+    # DS: exact names, and the wDefl-vanilla branch that calls an unimported function
+    assert engine.elastic_model("Ruth_vanilla", DS) == _lib.ELASTIC_RUTH
+    assert engine.elastic_model("Ruth_nigram", DS) == _lib.ELASTIC_NIGRAM
+    assert engine.elastic_model("Ruth_nigram_wDefl", DS) == _lib.ELASTIC_NIGRAM_WDEFL
+    with pytest.raises(NameError):
+        engine.elastic_model("Ruth_vanilla_wDefl", DS)
+    # continuous: substring tests, wDefl variants fall back to the base model
+    assert engine.elastic_model("Ruth_vanilla_wDefl", CONT) == _lib.ELASTIC_RUTH
+    assert engine.elastic_model("Ruth_nigram_wDefl", CONT) == _lib.ELASTIC_NIGRAM
+    # one-to-one mapping on request
+    for name, code in _lib.ELASTIC.items():
+        assert engine.elastic_model(name, DS, "intended") == code
+        assert engine.elastic_model(name, CONT, "intended") == code
+    with pytest.raises(NotImplementedError):
+        engine.elastic_model("Mott", DS)
+    with pytest.raises(ValueError):
+        engine.elastic_model("Ruth_other", DS)
+
+
+def test_diffraction_needs_extinction_distance():
+    from mcd import engine
+    p = config.parse_input(INPUT)
+    p.update(mode="DS", material="Si", diffMFP=True, thickness=3000.0)
+    s = engine.make_sim(p, 16)
+    assert s.diff_mfp == 1 and s.thickness == 3000.0
+    assert _lib.material("Si").xip_g == 1360.0
+    with pytest.raises(KeyError):
+        engine.make_sim(dict(p, material="Al"), 16)
+    # continuous mode has no diffraction channel (MC/tools/scattering.py:753-800)
+    assert engine.make_sim(dict(p, mode="cont"), 16).diff_mfp == 0
 
 
 def test_sim_struct_from_input():

@@ -28,6 +28,14 @@ def test_physics_functions(golden, sp):
     assert rel([mat.atnd, mat.plasmon_e, mat.fermi_e], P[sp + "/const"]) < 1e-14
     assert rel([O.alpha(e, mat.Z) for e in E], P[sp + "/alpha"]) < 1e-14
     assert rel([O.ruther_sigma(e, mat.Z) for e in E], P[sp + "/ruth"]) < 1e-14
+    assert rel([O.ruther_sigma_wDefl(e, mat.Z) for e in E], P[sp + "/ruth_wdefl"]) < 1e-14
+    assert rel([O.ruther_N_sigma(e, mat.Z) for e in E], P[sp + "/ruth_nigram"]) < 1e-14
+    assert rel([O.ruther_N_sigma_wDefl(e, mat.Z) for e in E], P[sp + "/ruth_nigram_wdefl"]) < 1e-14
+    if sp + "/xip_g" in P:
+        assert mat.xip_g == float(P[sp + "/xip_g"])
+        assert rel([O.diffr_sigma(mat.xip_g, mat.atnd)], [float(P[sp + "/diffr"])]) < 1e-14
+    else:
+        assert mat.xip_g is None
     for Wc in (10.0, 50.0, 100.0):
         assert rel([O.moller_sigma(e, Wc, mat.n_val) for e in E], P[sp + "/moller/%g" % Wc]) < 1e-14
     for name, Es, ns in mat.shells:
@@ -78,27 +86,41 @@ def _tables_for(T, name, mat):
     return out
 
 
-@pytest.mark.parametrize("tag,tname", [("ds_si", "cfg1"), ("ds_au", "cfg3"), ("cont_al", None), ("cont_cu", None)])
+REPLAYS = [("ds_si", "cfg1"), ("ds_au", "cfg3"), ("cont_al", None), ("cont_cu", None),
+           ("ds_si_nigram", "cfg1"), ("ds_si_nigram_wdefl", "cfg1"), ("ds_si_diff", "cfg1"),
+           ("cont_al_nigram", None)]
+
+
+@pytest.mark.parametrize("tag,tname", REPLAYS)
 def test_replay_reference_trajectories(golden, tag, tname):
     """Whole trajectories of the reference, replayed on its own MT19937 stream:
-    same channel sequence, same outcome rows, values within 1e-9."""
+    same channel sequence, same outcome rows, values within 1e-9.  Besides the
+    default model: Nigram elastic cross sections (DS and continuous), and the
+    diffraction channel of diffMFP in a 3000 A Si film, run by the reference
+    with its extinction distance supplied (its constructor reads self.xip_g,
+    whose assignment is commented out)."""
     R = golden["replay"]
     mat = O.Material(str(R[tag + "/species"]))
     cfg = R[tag + "/cfg"]
     evo, rwo = R[tag + "/ev_off"], R[tag + "/row_off"]
     tabs = _tables_for(golden["tables"], tname, mat) if tname else None
+    elastic = str(R[tag + "/elastic"]) if tag + "/elastic" in R else "Ruth_vanilla"
+    diff = bool(R[tag + "/diffMFP"]) if tag + "/diffMFP" in R else False
+    maxz = float(R[tag + "/thickness"]) if tag + "/thickness" in R else 1e30
     for k, seed in enumerate(R[tag + "/seeds"]):
         el = O.Electron(cfg[0], cfg[1], O.beam_direction(cfg[2]), record=True)
         if tag.startswith("ds"):
-            O.trajectory_ds(el, mat, cfg[3], 10 ** 9, 1e30, tabs, O.MTStream(int(seed)))
+            O.trajectory_ds(el, mat, cfg[3], 10 ** 9, maxz, tabs, O.MTStream(int(seed)), elastic, diff)
         else:
-            O.trajectory_cont(el, mat, 10 ** 9, 1e30, "classical", O.MTStream(int(seed)))
+            O.trajectory_cont(el, mat, 10 ** 9, maxz, "classical", O.MTStream(int(seed)), elastic=elastic)
         a, b = evo[k], evo[k + 1]
         assert len(el.events) == b - a
         ev = np.array(el.events, dtype=float)
         cols = [("E_loss", 2), ("pol_angle", 3), ("az_angle", 4), ("pathl", 5), ("energy", 9)]
         if tag.startswith("ds"):
-            assert np.array_equal(ev[:, 0].astype(int), R[tag + "/ev/type"][a:b])
+            types = R[tag + "/ev/type"][a:b].copy()
+            types[types == 3 + len(mat.shells)] = O.CH_DIFF     # the label list ends with 'diff'
+            assert np.array_equal(ev[:, 0].astype(int), types)
             cols += [("E", 1), ("x", 6), ("y", 7), ("z", 8)]
         for col, ci in cols:
             ref = R[tag + "/ev/" + col][a:b]
@@ -114,6 +136,13 @@ def test_replay_reference_trajectories(golden, tag, tname):
             assert np.allclose(d, [R[tag + "/row/" + c][ra + i] for c in ("dx", "dy", "dz")], rtol=0, atol=1e-9)
             assert np.allclose(p, [R[tag + "/row/" + c][ra + i] for c in ("last_x", "last_y", "last_z")],
                                rtol=1e-9, atol=1e-6)
+
+
+def test_diffraction_replay_reaches_trdf(golden):
+    """The diffraction fixture exercises the channel and the 'trdf' exit."""
+    R = golden["replay"]
+    assert (R["ds_si_diff/ev/type"] == 6).sum() >= 3
+    assert (R["ds_si_diff/row/outcome"] == "trdf").sum() >= 1
 
 
 def test_abs_row_keeps_pre_loss_energy(golden):
@@ -156,6 +185,20 @@ def test_c_oracle_equals_python_oracle(golden):
     assert np.array_equal([e.rows[0][2] for e in py], c["dir"])
     assert np.array_equal([e.rows[0][3] for e in py], c["last_pos"])
     assert np.array_equal([e.steps for e in py], c["n_events"])
+    # elastic variants and the diffraction channel in a Si film
+    for elastic, diff, th in (("Ruth_nigram", False, 1e30), ("Ruth_nigram_wDefl", False, 1e30),
+                              ("Ruth_vanilla_wDefl", False, 1e30), ("Ruth_vanilla", True, 3000.0)):
+        c = coracle.run(mat, 10000.0, 1000.0, 0.0, n, seed=5, mode="DS", Wc=100.0, tables=hts, nthreads=3,
+                        elastic=elastic, diff=diff, thickness=th)
+        py = O.run_ds(mat, 10000.0, 1000.0, 0.0, 100.0, 10 ** 15, th, pts, n, 5, elastic=elastic, diff=diff)
+        assert np.array_equal([O.OUT_CODE[e.rows[0][0]] for e in py], c["outcome"]), elastic
+        assert np.array_equal([e.rows[0][1] for e in py], c["final_E"]), elastic
+        assert np.array_equal([e.rows[0][2] for e in py], c["dir"]), elastic
+        assert np.array_equal([e.steps for e in py], c["n_events"]), elastic
+    m2 = O.Material("Al")
+    c = coracle.run(m2, 15000.0, 1000.0, 70.0, 8, seed=9, mode="cont", nthreads=2, elastic="Ruth_nigram")
+    py = O.run_cont(m2, 15000.0, 1000.0, 70.0, 10 ** 15, 1e30, "classical", 8, 9, elastic="Ruth_nigram")
+    assert np.array_equal([e.rows[0][1] for e in py], c["final_E"])
     for model in ("classical", "JL", "explicit"):
         m2 = O.Material("Cu")
         c = coracle.run(m2, 20000.0, 1000.0, 70.0, 8, seed=9, mode="cont", bethe=model, nthreads=2)
