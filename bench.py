@@ -288,6 +288,41 @@ def cont_bench(args, dev):
             "gpu_launches": 2 * args.steps}
 
 
+DET_WORKLOAD = ("projection of 2^27 float32 exit directions (three planes, 1.61 GB) onto the EBSD detector "
+                "(two planes, 1.07 GB out), reference geometry")
+
+
+def detector_bench(args, dev):
+    """HBM roofline of the detector projection map: 20 algorithmic bytes per
+    direction (12 read, 8 written), inputs far larger than L2."""
+    import torch
+    from mcd import detector
+    n = max(1 << 20, int(round((1 << 27) * args.scale)))
+    g = torch.Generator(device=dev).manual_seed(args.seed)
+    dirs = torch.randn((3, n), generator=g, device=dev, dtype=torch.float32)
+    dirs /= dirs.norm(dim=0, keepdim=True)
+    out = torch.empty((2, n), device=dev, dtype=torch.float32)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        detector.project(dirs, out=out)
+    torch.cuda.synchronize(dev)
+    times = []
+    for _ in range(max(3, args.steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        detector.project(dirs, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    t = statistics.median(times)
+    peak = float(measured_peaks().get("hbm_gbs", 6800.0))
+    gbs = 20.0 * n / t / 1e9
+    return {"workload": DET_WORKLOAD, "n": n, "ms": t * 1e3, "directions_per_s": n / t,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "bytes_per_direction": 20, "peak_note": "measured copy bandwidth"},
+            "gpu_launches": max(3, args.steps)}
+
+
 STREAM_WORKLOAD = ("DS Au, E0 30 keV, Emin 0.5 keV, tilt 70 deg, Wc 50 eV, tol 1e-4, every event streamed "
                    "as a 40-byte record through two device rings to pinned host memory")
 
@@ -464,6 +499,7 @@ def run_mcd(args):
     adj = None if args.no_adjoint else adjoint_bench(args, dev)
     stream = None if args.no_stream else stream_bench(args, dev)
     cont = None if args.no_cont else cont_bench(args, dev)
+    det = None if args.no_detector else detector_bench(args, dev)
     if args.no_cpu:
         cpu = {"events": 0, "times": [float("nan")], "threads": 0}
     else:
@@ -498,6 +534,7 @@ def run_mcd(args):
         "adjoint": adj,
         "stream": stream,
         "cont": cont,
+        "detector": det,
         "gpu_launches": K,
         "status": status,
     }
@@ -522,6 +559,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (bwd/fwd) measurement")
     ap.add_argument("--no-stream", action="store_true", help="skip the streamed-event measurement")
     ap.add_argument("--no-cont", action="store_true", help="skip the continuous-mode histogram measurement")
+    ap.add_argument("--no-detector", action="store_true", help="skip the detector-projection measurement")
     ap.add_argument("--stream-fraction", type=float, default=1.0,
                     help="fraction of the 1e7-electron streaming workload to run (1 = all of it)")
     args = ap.parse_args()

@@ -339,6 +339,19 @@ int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims,
                             const int32_t* sim_gryz, mcd_tally* tallies,
                             const mcd_tune* tune, uint32_t* status, void* stream);
 
+/* Exit directions -> detector coordinates, replacing projOnDetector
+ * (MC/tools/rotation.py:78-102) with the detector geometry of
+ * MC/tools/parameters.py:22-33 supplied by the caller.  dir holds n
+ * directions as three planes dx[n], dy[n], dz[n] (the mcd_electron_out.dir
+ * layout); xy receives x[n], y[n]:
+ *     x = dx - x_pc,  y = R_x(-alpha)[1] . d - y_pc,
+ * the rotation taken from the conjugate of q = (cos(alpha/2), sin(alpha/2),
+ * 0, 0) as the reference does; L (the z translation) does not reach x, y.
+ * precision is MCD_FP32 (float planes, FP32 arithmetic) or MCD_FP64.
+ * Device pointers, stream-ordered; n == 0 launches nothing.              */
+int mcd_project_detector(const void* dir, int64_t n, int32_t precision, double alpha_deg,
+                         double x_pc, double y_pc, double L, void* xy, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -217,6 +217,8 @@ SIGNATURES = {
     "mcd_run_batched_noalloc": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
                                           C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.c_void_p, C.POINTER(Tune), C.c_void_p, C.c_void_p]),
+    "mcd_project_detector": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_void_p, C.c_void_p]),
     "mcd_run_batched_ring": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(Tune), C.POINTER(EventRing),
                                        C.c_void_p, C.c_void_p]),
     "mcd_adjoint_forward": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(SoftHist),

@@ -19,7 +19,7 @@ BUILD_DIR = os.path.join(ROOT, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-SOURCES = ["mcd_host.cpp", "mcd_tables.cu", "mcd_transport.cu", "mcd_adjoint.cu"]
+SOURCES = ["mcd_host.cpp", "mcd_tables.cu", "mcd_transport.cu", "mcd_adjoint.cu", "mcd_detector.cu"]
 EXTRA = {
     # FP32 transport: approximate division/sqrt and flush-to-zero; FP64 and the
     # accurate logf of the step length are unaffected by these flags.

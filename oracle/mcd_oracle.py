@@ -648,3 +648,26 @@ def run_cont(mat, E0, Emin, s_tilt, maxScatt, maxz, model, n_el, seed, sim=0, fi
         trajectory_cont(el, mat, maxScatt, maxz, model, PhiloxStream(seed, k, sim), status, J, n, elastic)
         out.append(el)
     return out
+
+
+# --------------------------------------------------------------------------
+# detector projection
+# --------------------------------------------------------------------------
+def proj_on_detector(xyz_exit, alpha, xy_PC, L):
+    """rotation.py:78-102: rotate each direction by conj(q_SD), q_SD =
+    (cos(alpha/2), sin(alpha/2), 0, 0), through the rotation matrix of a
+    quaternion (entries / |q|^2, as numpy-quaternion's rotate_vectors),
+    subtract t = (x_PC, y_PC, L), keep x and y.  Returns an (n, 2) array."""
+    c = math.cos(math.radians(alpha) / 2.0)
+    s = (1.0 - c * c) ** 0.5
+    w, x, y, z = c, -s, 0.0, 0.0
+    n = w * w + x * x + y * y + z * z
+    m = np.array([
+        [1.0 - 2.0 * (y * y + z * z) / n, 2.0 * (x * y - z * w) / n, 2.0 * (x * z + y * w) / n],
+        [2.0 * (x * y + z * w) / n, 1.0 - 2.0 * (x * x + z * z) / n, 2.0 * (y * z - x * w) / n],
+        [2.0 * (x * z - y * w) / n, 2.0 * (y * z + x * w) / n, 1.0 - 2.0 * (x * x + y * y) / n],
+    ])
+    v = np.asarray(xyz_exit, dtype=np.float64).reshape(-1, 3)
+    t = np.array([xy_PC[0], xy_PC[1], L], dtype=np.float64)
+    return (v @ m.T - t)[:, 0:2]
+

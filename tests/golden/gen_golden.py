@@ -127,6 +127,20 @@ def part_physics():
             c2.append(sc.Rutherford_halfPol(E, p["Z"]))
         out[spc + "/ruth_EU"] = np.array(us)
         out[spc + "/ruth_c2"] = np.array(c2)
+    # detector projection (MC/tools/rotation.py:78-102) of seeded unit
+    # directions and the axes, at the geometry of MC/tools/parameters.py:22-33
+    # and at other tilts
+    rng = np.random.default_rng(11)
+    d = rng.normal(size=(61, 3))
+    d = np.vstack([d / np.linalg.norm(d, axis=1)[:, None], np.eye(3), -np.eye(3)])
+    xy_pc = np.asarray(m["parameters"].xy_PC, dtype=np.float64)
+    out["det/dirs"] = d
+    out["det/xy_PC"] = xy_pc
+    out["det/L"] = np.array(float(m["parameters"].L))
+    out["det/alphas"] = np.array([float(m["parameters"].alpha), 0.0, 45.0, 70.0, 90.0, 180.0])
+    for a in out["det/alphas"]:
+        res = m["rotation"].projOnDetector(list(d), a, xy_pc, out["det/L"])
+        out["det/xy/%g" % a] = np.asarray(res, dtype=np.float64)
     np.savez_compressed(os.path.join(HERE, "physics.npz"), **out)
     print("physics.npz:", len(out), "arrays")
 

@@ -56,6 +56,15 @@ def test_physics_functions(golden, sp):
     assert rel([O.maxW(e, mat.fermi_e) for e in EE[:, 0]], P[sp + "/maxW"]) < 1e-15
 
 
+def test_detector_projection_matches_reference(golden):
+    """rotation.py:78-102 at the geometry of parameters.py:22-33 and at other
+    tilts, on seeded unit directions and the six axis directions."""
+    P = golden["physics"]
+    for a in P["det/alphas"]:
+        got = O.proj_on_detector(P["det/dirs"], a, P["det/xy_PC"], float(P["det/L"]))
+        assert np.max(np.abs(got - P["det/xy/%g" % a])) <= 1e-12 * 6000.0, a
+
+
 def test_table_cdf_matches_reference(golden):
     """Every table the benchmarks sample: unmasked counts exact, values within
     one float32 step of the reference's table (the reference evaluates parts
