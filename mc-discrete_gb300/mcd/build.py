@@ -21,8 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 SOURCES = ["mcd_host.cpp", "mcd_tables.cu", "mcd_transport.cu", "mcd_adjoint.cu", "mcd_detector.cu"]
 EXTRA = {
-    # FP32 transport: approximate division/sqrt and flush-to-zero; FP64 and the
-    # accurate logf of the step length are unaffected by these flags.
+    # FP32 transport: approximate division/sqrt and flush-to-zero; FP64
+    # transport is unaffected by these flags.
     "mcd_transport.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false", "-Xptxas", "-v"],
     "mcd_adjoint.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false", "--extended-lambda"],
 }
