@@ -25,11 +25,10 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
             k0 += 0x9E3779B9u;
             k1 += 0xBB67AE85u;
         }
-        const uint32_t lo0 = 0xD2511F53u * c.x;
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x);
-        const uint32_t lo1 = 0xCD9E8D57u * c.z;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z);
-        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+        // one 32 x 32 -> 64-bit product per multiplier
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1, (uint32_t)p0);
     }
     return c;
 }
@@ -42,12 +41,15 @@ struct Ops;
 
 template <>
 struct Ops<float> {
-    // uniform in (0,1) from the top 23 bits, and its exact complement 1 - U
+    // uniform in (0,1) from the top 23 bits, (u >> 9) 2^-23 + 2^-24, and its
+    // exact complement 1 - U.  The 23 bits become the mantissa of a float in
+    // [1, 2); subtracting 1 - 2^-24 is exact (Sterbenz), so no integer to
+    // float conversion is needed.
     static __device__ __forceinline__ float unit(uint32_t u) {
-        return (float)(u >> 9) * 0x1p-23f + 0x1p-24f;
+        return __uint_as_float((u >> 9) | 0x3f800000u) - 0x1.fffffep-1f;
     }
     static __device__ __forceinline__ float unit_c(uint32_t u) {
-        return (float)((~u) >> 9) * 0x1p-23f + 0x1p-24f;
+        return __uint_as_float(((~u) >> 9) | 0x3f800000u) - 0x1.fffffep-1f;
     }
     static __device__ __forceinline__ float ln(float x) { return __logf(x); }
     // logarithm of the step-length draw: the special-function unit's log2,
