@@ -277,7 +277,13 @@ __device__ __forceinline__ void lane_lose(Lane<T>& L, const C& c, T W) {
 
 // Direction update (MC/tools/electron.py:87-99, MC/tools/rotation.py:41-53):
 // q = q_az * q_pol with q_pol = (cos t/2, y sin t/2), q_az = (cos h, d sin h),
-// applied to d and y, each renormalised.  s2 = sin^2(theta/2).
+// applied to d and y, each renormalised.  s2 = sin^2(theta/2).  With y
+// perpendicular to d (true initially and kept by every update), q_pol turns
+// d about y by theta and q_az then turns both vectors about the old d by
+// phi = 2h; in the frame (d, y, x = y cross d) that is
+//     d' = d cos(theta) + sin(theta) (x cos(phi) + y sin(phi)),
+//     y' = y cos(phi) - x sin(phi),
+// the rotation q p q* written out (equal to it within rounding).
 template <class T, class C>
 __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_phi) {
     const T st = Ops<T>::sqrt_(s2);
@@ -285,34 +291,19 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_ph
     T sp, cp;
     Ops<T>::sincos_pi(u_phi, &sp, &cp);
     if (c.quirks & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
-    const T dy_ = L.dx * L.yx + L.dy * L.yy + L.dz * L.yz;
-    // cross d x y
-    const T cx = L.dy * L.yz - L.dz * L.yy;
-    const T cy = L.dz * L.yx - L.dx * L.yz;
-    const T cz = L.dx * L.yy - L.dy * L.yx;
-    const T w = cp * ct - sp * st * dy_;
-    const T a = cp * st, b = ct * sp, e = sp * st;
-    const T vx = a * L.yx + b * L.dx + e * cx;
-    const T vy = a * L.yy + b * L.dy + e * cy;
-    const T vz = a * L.yz + b * L.dz + e * cz;
-    // p' = p + w t + v x t,  t = 2 v x p
+    const T cth = (T)1 - (T)2 * s2, sth = (T)2 * st * ct;
+    const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
+    const T xx = L.yy * L.dz - L.yz * L.dy;
+    const T xy = L.yz * L.dx - L.yx * L.dz;
+    const T xz = L.yx * L.dy - L.yy * L.dx;
+    const T a = sth * cph, b = sth * sph;
     T nd[3], ny[3];
-    {
-        const T tx = (T)2 * (vy * L.dz - vz * L.dy);
-        const T ty = (T)2 * (vz * L.dx - vx * L.dz);
-        const T tz = (T)2 * (vx * L.dy - vy * L.dx);
-        nd[0] = L.dx + w * tx + (vy * tz - vz * ty);
-        nd[1] = L.dy + w * ty + (vz * tx - vx * tz);
-        nd[2] = L.dz + w * tz + (vx * ty - vy * tx);
-    }
-    {
-        const T tx = (T)2 * (vy * L.yz - vz * L.yy);
-        const T ty = (T)2 * (vz * L.yx - vx * L.yz);
-        const T tz = (T)2 * (vx * L.yy - vy * L.yx);
-        ny[0] = L.yx + w * tx + (vy * tz - vz * ty);
-        ny[1] = L.yy + w * ty + (vz * tx - vx * tz);
-        ny[2] = L.yz + w * tz + (vx * ty - vy * tx);
-    }
+    nd[0] = L.dx * cth + xx * a + L.yx * b;
+    nd[1] = L.dy * cth + xy * a + L.yy * b;
+    nd[2] = L.dz * cth + xz * a + L.yz * b;
+    ny[0] = L.yx * cph - xx * sph;
+    ny[1] = L.yy * cph - xy * sph;
+    ny[2] = L.yz * cph - xz * sph;
     const T rd = Ops<T>::rsqrt_(nd[0] * nd[0] + nd[1] * nd[1] + nd[2] * nd[2]);
     const T ry = Ops<T>::rsqrt_(ny[0] * ny[0] + ny[1] * ny[1] + ny[2] * ny[2]);
     L.dx = nd[0] * rd;
