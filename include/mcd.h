@@ -251,9 +251,11 @@ int mcd_run(const mcd_sim* sim, const mcd_material* mat,
  * work queue.  mcd_batch_prepare packs the simulations into a caller-owned
  * device workspace of mcd_batch_workspace_bytes(nsims) bytes (host-to-device
  * copy on `stream`; host memory may be reused when the call returns) and
- * builds there, per DS simulation, a 4096-point log-energy table of the
- * cumulative channel cross sections (FP64 evaluation, FP32 storage) that the
- * kernel interpolates instead of evaluating 3 + n_shells formulas per event.
+ * builds there log-energy tables of E times the cumulative channel cross
+ * sections (FP64 evaluation, FP32 storage, 128 points per octave, one table
+ * per group of DS simulations with the same material, Wc and density) that
+ * the kernel interpolates instead of evaluating 3 + n_shells formulas per
+ * event (tune variant bit 1 keeps the formulas).
  * mcd_run_batched then only resets the queue and launches, so it can be
  * captured in a CUDA graph.  tallies[nsims] and status are device pointers.
  * Replaces MapScatterer.__call__ (MC/doScatter.py:54-95) with its pool of

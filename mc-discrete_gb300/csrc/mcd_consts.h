@@ -98,9 +98,9 @@ struct SimConst {
     // kernel only; nullptr = evaluate inline).  Row i (of sig_rows, sig_S
     // floats apart) holds, at E = 2^(sig_l0 + i / sig_inv), E times the
     // running sums over the channels in pick order: Ruth, Moller,
-    // Gryz[0..nsh-1], Quinn (sig_K = nsh + 3 columns).  E * sigma varies
-    // slowly in log E, so linear interpolation at 256 rows per octave is
-    // within 2e-7 of the exact sums (relative to the total).
+    // Gryz[0..nsh-1], Quinn (sig_K = nsh + 3 columns; padding FLT_MAX).
+    // E * sigma varies slowly in log E, so linear interpolation at 128 rows
+    // per octave is within 3e-7 of the exact sums (relative to the total).
     const float* sig;
     float sig_l0, sig_inv, sig_tmax;
     int32_t sig_K, sig_S, sig_rows;
@@ -108,7 +108,7 @@ struct SimConst {
 
 constexpr int kSigRowsMax = 4096;      // grid points of a cross-section table, at most
 constexpr int kSigStride = 12;         // floats per row, at most (3 + MCD_MAX_SHELLS + 1)
-constexpr double kSigPerOctave = 256;  // grid density
+constexpr double kSigPerOctave = 128;  // grid density
 
 // Host-side builder: precompute the constant block of one simulation.
 template <class T>

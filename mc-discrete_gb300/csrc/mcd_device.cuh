@@ -337,21 +337,19 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     *Etot_out = all;
     const float target = U * all;
     if (c.diff && target > tot) return MCD_CH_DIFF;
-    int j = K - 1;
+    // the running sums increase along the row (padding holds FLT_MAX), so
+    // the first column >= target is the number of columns below it
+    int j = 0;
 #pragma unroll
     for (int q = 0; q < kSigStride / 4; ++q) {
         if (4 * q < S) {
             const float4 x = __ldg(reinterpret_cast<const float4*>(r0) + q);
             const float4 y = __ldg(reinterpret_cast<const float4*>(r1) + q);
-            const float v[4] = {fmaf(f, y.x - x.x, x.x), fmaf(f, y.y - x.y, x.y), fmaf(f, y.z - x.z, x.z),
-                                fmaf(f, y.w - x.w, x.w)};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int col = 4 * q + e;
-                if (col < j && target <= v[e]) j = col;
-            }
+            j += (fmaf(f, y.x - x.x, x.x) < target) + (fmaf(f, y.y - x.y, x.y) < target) +
+                 (fmaf(f, y.z - x.z, x.z) < target) + (fmaf(f, y.w - x.w, x.w) < target);
         }
     }
+    j = j < K - 1 ? j : K - 1;
     // column -> channel code: 0 Ruth, 1 Moller, 2..K-2 Gryz[k], K-1 Quinn
     if (j == 0) return MCD_CH_RUTH;
     if (j == 1) return MCD_CH_MOLLER;

@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
     }
     cum += sig_quinn<double>(c, E, invE);
     row[col++] = (float)(E * cum);
-    for (; col < cf.sig_S; ++col) row[col] = 0.0f;
+    for (; col < cf.sig_S; ++col) row[col] = 3.402823466e38f;   // padding: never below a target
 }
 
 // Do two simulations have the same channel cross sections at every energy?
