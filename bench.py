@@ -368,7 +368,7 @@ def run_mcd(args):
 
     batch = engine.Batch(sims, seed=args.seed, device=dev, first_electron=first)
     if args.block or args.refill:
-        tune = _lib.Tune(args.block or 256, args.blocks_per_sm, args.refill or 1, 0, 0)
+        tune = _lib.Tune(args.block or 256, args.blocks_per_sm, args.refill or 1, args.variant, 0)
         tune_table = None
     else:
         tune, tune_table = autotune.tune(batch)
@@ -550,6 +550,7 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="batched block size (0: autotune)")
     ap.add_argument("--refill", type=int, default=0, help="batched refill granularity (0: autotune)")
     ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=0, help="batched tune variant bits, with --block")
     ap.add_argument("--plain-block", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--scale", type=float, default=1.0,

@@ -20,12 +20,12 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 3
+#define MCD_ABI_VERSION 4
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
 #define MCD_HIST_T_MAX 180
-#define MCD_GUIDE 32           /* guide entries per table row (see mcd_table) */
+#define MCD_GUIDE 256          /* guide buckets per table row (see mcd_table) */
 
 /* ---- return codes ------------------------------------------------------ */
 enum {
@@ -109,9 +109,11 @@ typedef struct mcd_table {
     const float* Ws;         /* device, nW energy losses (float32 geomspace)  */
     const float* cdf;        /* device, nE x (nW-1); 0 marks a masked entry   */
     const int32_t* nvalid;   /* device, nE unmasked counts per row, or NULL   */
-    const int32_t* guide;    /* device, nE x (MCD_GUIDE+1): first CDF index
-                                whose value is >= k/MCD_GUIDE, or NULL; it
-                                narrows the search without changing its result */
+    const uint16_t* guide;   /* device, nE x (MCD_GUIDE+1): first CDF index
+                                whose value is >= k/MCD_GUIDE, or NULL (needs
+                                nW - 1 <= 65535); a draw U lies between entries
+                                floor(U G) and floor(U G) + 1, so most draws
+                                need no CDF read; the result is unchanged   */
     int32_t nE;
     int32_t nW;
     float E_first;           /* Es[0] and Es[nE-1] as the host holds them, so */
@@ -231,7 +233,7 @@ int mcd_device_info(int* sm_count, int* cc_major, int* cc_minor);
  * Replaces probTable.computeBlock/generate (MC/tools/probTables.py:415-486). */
 int mcd_build_table(int kind, const mcd_material* mat, int shell,
                     int32_t nE, int32_t nW, const float* Es, const float* Ws,
-                    float* cdf32, double* cdf64, int32_t* nvalid, int32_t* guide,
+                    float* cdf32, double* cdf64, int32_t* nvalid, uint16_t* guide,
                     void* stream);
 
 /* One simulation, one GPU thread per electron, one launch.

@@ -51,7 +51,7 @@ struct TableDev {
     const float* Ws;
     const float* cdf;
     const int32_t* nvalid;
-    const int32_t* guide;
+    const uint16_t* guide;
     int32_t nE;
     int32_t nW;
     float E_first, E_last;

@@ -181,9 +181,10 @@ __device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) 
     const float* row = t.cdf + (size_t)i * ncol;
     int lo, hi;
     if (t.guide) {
-        // the answer lies between the first entries >= k/G and >= (k+1)/G
+        // the answer lies between the first entries >= k/G and >= (k+1)/G,
+        // usually the same column (no CDF read at all)
         const int k = (int)(U * (T)MCD_GUIDE);
-        const int32_t* g = t.guide + (size_t)i * (MCD_GUIDE + 1) + k;
+        const uint16_t* g = t.guide + (size_t)i * (MCD_GUIDE + 1) + k;
         lo = __ldg(g);
         hi = __ldg(g + 1);
     } else {

@@ -25,7 +25,7 @@ struct FillParams {
     float* cdf32;
     double* cdf64;
     int32_t* nvalid;
-    int32_t* guide;
+    uint16_t* guide;
     int32_t nE, nW;
     int32_t kind;
     double nfree;  // Moller: valence electrons; Gryzinski: shell occupancy
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(256) k_fill(const FillParams p) {
                 const float v = r[mid];
                 if (v != 0.0f && v < q) lo = mid + 1; else hi = mid;
             }
-            p.guide[(size_t)row * (MCD_GUIDE + 1) + k] = lo;
+            p.guide[(size_t)row * (MCD_GUIDE + 1) + k] = (uint16_t)lo;
         }
     }
 }
@@ -132,9 +132,10 @@ using namespace mcd;
 
 extern "C" int mcd_build_table(int kind, const mcd_material* mat, int shell, int32_t nE, int32_t nW,
                                const float* Es, const float* Ws, float* cdf32, double* cdf64, int32_t* nvalid,
-                               int32_t* guide, void* stream) {
+                               uint16_t* guide, void* stream) {
     if (!mat || !Es || !Ws || !cdf32) return MCD_EINVAL;
     if (nE < 1 || nW < 2) return MCD_EINVAL;
+    if (guide && nW - 1 > 65535) return MCD_EINVAL;   // column indices must fit 16 bits
     if (kind != MCD_TABLE_MOLLER && kind != MCD_TABLE_GRYZ) return MCD_EINVAL;
     FillParams p;
     p.Es = Es;

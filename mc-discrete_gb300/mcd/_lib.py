@@ -9,9 +9,9 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 MAX_SHELLS = 8
-GUIDE = 32
+GUIDE = 256
 MAX_CHANNELS = 16
 HIST_E_MAX = 256
 HIST_T_MAX = 180

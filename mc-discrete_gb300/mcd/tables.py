@@ -223,7 +223,10 @@ class DeviceTable:
         self.Es = torch.from_numpy(self.Es_host).to(self.device)
         self.cdf = torch.empty((self.nE, self.nW - 1), dtype=torch.float32, device=self.device)
         self.nvalid = torch.empty(self.nE, dtype=torch.int32, device=self.device)
-        self.guide = torch.empty((self.nE, _lib.GUIDE + 1), dtype=torch.int32, device=self.device)
+        # uint16 column indices (held in an int16 tensor of the same bytes);
+        # rows wider than 65535 columns go without a guide
+        self.guide = (torch.empty((self.nE, _lib.GUIDE + 1), dtype=torch.int16, device=self.device)
+                      if self.nW - 1 <= 65535 else None)
         self.cdf64 = (torch.empty((self.nE, self.nW - 1), dtype=torch.float64, device=self.device)
                       if keep_fp64 else None)
         st = stream if stream is not None else torch.cuda.current_stream(self.device)
@@ -232,10 +235,11 @@ class DeviceTable:
             _lib.C.byref(mat), mat.n_shells - 1, self.nE, self.nW,
             self.Es.data_ptr(), self.Ws.data_ptr(), self.cdf.data_ptr(),
             self.cdf64.data_ptr() if self.cdf64 is not None else None,
-            self.nvalid.data_ptr(), self.guide.data_ptr(), st.cuda_stream)
+            self.nvalid.data_ptr(), self.guide.data_ptr() if self.guide is not None else None, st.cuda_stream)
         _lib.check("mcd_build_table", code)
         self.struct = _lib.Table(self.Es.data_ptr(), self.Ws.data_ptr(), self.cdf.data_ptr(),
-                                 self.nvalid.data_ptr(), self.guide.data_ptr(), self.nE, self.nW,
+                                 self.nvalid.data_ptr(), self.guide.data_ptr() if self.guide is not None else None,
+                                 self.nE, self.nW,
                                  float(self.Es_host[0]), float(self.Es_host[-1]))
 
 
