@@ -156,16 +156,11 @@ __device__ __forceinline__ int table_row(const TableDev& t, T E, bool* out_of_ra
     int g = (int)ceil((E - (T)e0) * (T)(nE - 1) / (T)(eL - e0));
     g = g < 1 ? 1 : (g > nE - 1 ? nE - 1 : g);
     int lo = 0, hi = nE - 1;  // invariant: Es[lo] < E <= Es[hi]
-    for (int it = 0; it < 4; ++it) {
-        if ((T)__ldg(t.Es + g) >= E) {
-            hi = g;
-            if ((T)__ldg(t.Es + g - 1) < E) return g;
-            --g;
-        } else {
-            lo = g;
-            ++g;
-        }
-        if (g <= lo || g > hi) break;
+    {
+        // both neighbours of the guess in one round trip
+        const T a = (T)__ldg(t.Es + g - 1), b = (T)__ldg(t.Es + g);
+        if (a < E && E <= b) return g;
+        if (b < E) lo = g; else hi = g - 1;
     }
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
