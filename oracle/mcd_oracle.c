@@ -1,7 +1,7 @@
 /*
  * mcd_oracle.c - FP64 CPU oracle of the electron-trajectory Monte Carlo.
  *
- * TEST INFRASTRUCTURE ONLY: the checker and the CPU baseline.  It is built
+ * TEST INFRASTRUCTURE ONLY: the parity reference and the CPU baseline.  It is built
  * by oracle/Makefile into oracle/_build/libmcd_oracle.so and loaded by the
  * tests and by bench.py's CPU leg; the library under mc-discrete_gb300/
  * never links or calls it.

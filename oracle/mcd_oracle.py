@@ -1,6 +1,6 @@
 """CPU oracle for the electron-trajectory Monte Carlo (FP64 restatement).
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: tests/, the smoke check
+TEST INFRASTRUCTURE ONLY.  This module is the parity reference: tests/, the smoke check
 in __graft_entry__ and the CPU-baseline leg of bench.py may import it; the
 library under mc-discrete_gb300/ never does.
 
