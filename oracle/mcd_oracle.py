@@ -671,3 +671,65 @@ def proj_on_detector(xyz_exit, alpha, xy_PC, L):
     t = np.array([xy_PC[0], xy_PC[1], L], dtype=np.float64)
     return (v @ m.T - t)[:, 0:2]
 
+
+# --------------------------------------------------------------------------
+# theory distributions and the two-sample test of the reference's tests
+# --------------------------------------------------------------------------
+def ruth_theta_ppf(x, E, Z):
+    """distributions.py:400-416 (Ruth_diffCS_E._ppf): polar angle in degrees
+    of the Rutherford distribution at energy E for uniform x."""
+    a = alpha(np.asarray(E, dtype=np.float64), Z)
+    x = np.asarray(x, dtype=np.float64)
+    return np.degrees(np.arccos(1.0 - (2.0 * a * x) / (1.0 + a - x)))
+
+
+def theory_W_cdf(kind, mat, E, Wmin, npts=20001):
+    """distributions.py:21-124: CDF of the energy loss at energy E from
+    dsigma/dW between Wmin and maxW(E) (Moller: valence electrons; Gryz: the
+    outermost shell, Wmin its binding energy).  Integrated on a geometric W
+    grid by the trapezoid rule in ln W; returns (W grid, CDF)."""
+    Wmax = maxW(E, mat.fermi_e)
+    W = np.geomspace(Wmin, Wmax, npts)
+    if kind == "Moller":
+        f = moller_dcs(E, W, mat.n_val)
+    else:
+        _, Eb, ns = mat.outer_shell
+        f = gryz_dcs(E, W, ns, Eb)
+    g = f * W
+    c = np.concatenate([[0.0], np.cumsum(0.5 * (g[1:] + g[:-1]) * np.diff(np.log(W)))])
+    return W, c / c[-1]
+
+
+def theory_W_sample(kind, mat, E, Wmin, u, npts=20001):
+    """Inverse-CDF samples of the energy loss at energy E for uniforms u."""
+    W, c = theory_W_cdf(kind, mat, E, Wmin, npts)
+    return np.interp(np.asarray(u, dtype=np.float64), c, W)
+
+
+def theta_from_c2(c2):
+    """tests/testThings.py:153-161: degrees from cos^2(theta/2)."""
+    return np.degrees(2.0 * np.arccos(np.asarray(c2, dtype=np.float64) ** 0.5))
+
+
+def watson_u2(x, y):
+    """Two-sample Watson U^2 as tests/testThings.py:255-316 computes it
+    (Mardia and Jupp, Directional Statistics, eq. 8.3.7): over the sorted
+    unique pooled values, d_k = F_x - F_y, U^2 = nx ny (sum d^2 - (sum d)^2
+    / N) / N^2."""
+    x = np.sort(np.asarray(x, dtype=np.float64))
+    y = np.sort(np.asarray(y, dtype=np.float64))
+    nx, ny = x.size, y.size
+    N = nx + ny
+    t = np.unique(np.concatenate([x, y]))
+    d = np.searchsorted(x, t, side="right") / nx - np.searchsorted(y, t, side="right") / ny
+    return nx * ny * (np.sum(d * d) - np.sum(d) ** 2 / N) / N ** 2
+
+
+def watson_u2_pvalue(u2, terms=50):
+    """Asymptotic upper tail of U^2: 2 sum_k (-1)^(k-1) exp(-2 k^2 pi^2 u)
+    (the reference's critical value 0.152 is its 10% point)."""
+    if u2 <= 1e-4:        # the alternating series needs more terms there; the tail is 1
+        return 1.0
+    k = np.arange(1, terms + 1)
+    return float(min(1.0, max(0.0, 2.0 * np.sum((-1.0) ** (k - 1) * np.exp(-2.0 * k * k * PI * PI * u2)))))
+
