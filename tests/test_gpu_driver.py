@@ -1,0 +1,52 @@
+"""The whole-simulation driver on the GPU: `python -m mcd -i input.file`
+writes the reference's input / els / scats tables (here as .npz; HDF5 where
+pandas and PyTables exist), consistent with the run's own tallies."""
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from mcd import config, doScatter, engine
+
+pytestmark = pytest.mark.gpu
+
+INPUT = """num_el   : 3000
+E0       : 10000
+Emin     : 1000
+material : Si
+s_tilt   : 0
+mode     : DS
+Wc       : 100
+tol_E    : 1e-3
+tol_W    : 1e-3
+maxScatt : 100000
+electron_output : outcome, final_E, final_dir, last_pos
+scatter_output : type, E, E_loss, pol_angle, az_angle, pathl, position, energy
+"""
+
+
+def test_cli_writes_reference_tables(tmp_path):
+    f = tmp_path / "input.file"
+    f.write_text(INPUT)
+    out = str(tmp_path / "data") + "/"
+    root = __file__.rsplit("/tests/", 1)[0]
+    r = subprocess.run([sys.executable, "-m", "mcd", "-i", str(f), "-o", out, "--format", "npz", "--chunk", "1000"],
+                       cwd=root + "/mc-discrete_gb300", capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    p = config.readInput(str(f))
+    name = doScatter.store_name(config.with_defaults(p), out, ".npz")
+    z = np.load(name)
+    assert str(z["input/material"]) == "Si" and str(z["input/num_el"]) == "3000"
+    oc = z["els/outcome"]
+    g = engine.run(p, num_el=3000, seed=0)          # the same electrons: indices 0..2999, seed 0
+    t = g.tally
+    assert (oc == "bks").sum() == t["bks"] and (oc == "abs").sum() == t["abs"] + t["double_rows"]
+    assert oc.size == 3000 + t["double_rows"]
+    assert z["scats/type"].size == t["events"]
+    for c in ("E", "E_loss", "pol_angle", "az_angle", "pathl", "x", "y", "z", "energy"):
+        assert z["scats/" + c].size == t["events"], c
+    assert set(np.unique(z["scats/type"])) <= {"Ruth", "Moller", "Quinn", "Gryz1s", "Gryz2s", "Gryz2p"}
+    assert np.allclose(z["scats/energy"], z["scats/E"] - z["scats/E_loss"])
+    for c in ("dx", "dy", "dz", "last_x", "last_y", "last_z", "final_E"):
+        assert z["els/" + c].size == oc.size
