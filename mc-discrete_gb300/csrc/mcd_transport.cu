@@ -230,9 +230,11 @@ template <int MODE_MIX, bool REC, int MINB>
 __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
                                              const mcd_event_ring& ring, int inline_sigma);
 
-// Two register budgets of the same kernel: up to 1024 threads per block (64
-// registers, 4 blocks of 256 per SM), or 5 blocks of 256 per SM (48
-// registers, a few spilled values; more warps to hide latency).
+// Two register budgets of the same kernel: up to 1024 threads per block at
+// 64 registers (32 warps per SM: one block of 1024, the tuned shape on the
+// 64-simulation workload), or 5 blocks of 256 per SM at 48 registers (40
+// warps, a few spilled values, and five copies of the constant blocks in
+// shared memory, which take L1 capacity).
 template <int MODE_MIX, bool REC = false>
 __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallies, int refill,
                                                   uint32_t* status, const mcd_event_ring ring = mcd_event_ring{},
