@@ -93,7 +93,7 @@ struct SimConst {
     int64_t num_el;
     int32_t hE, hT;
     T invWE, invWT;  // 1/bin width (eV, degrees)
-    TableDev tm, tg;
+    TableDev tab[2];   // [0] Moller (valence), [1] Gryzinski (outermost shell)
     // cumulative channel cross sections tabulated on a log-E grid (batched
     // kernel only; nullptr = evaluate inline).  Row i (of sig_rows, sig_S
     // floats apart) holds, at E = 2^(sig_l0 + i / sig_inv), E times the
@@ -195,8 +195,8 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     c.invWE = (T)(s.hist_E_width > 0 ? 1.0 / s.hist_E_width : 0.0);
     c.invWT = (T)(s.hist_T_width > 0 ? 1.0 / s.hist_T_width : 0.0);
     TableDev z{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0.0f, 0.0f};
-    c.tm = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->guide, tm->nE, tm->nW, tm->E_first, tm->E_last} : z;
-    c.tg = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->guide, tg->nE, tg->nW, tg->E_first, tg->E_last} : z;
+    c.tab[0] = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->guide, tm->nE, tm->nW, tm->E_first, tm->E_last} : z;
+    c.tab[1] = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->guide, tg->nE, tg->nW, tg->E_first, tg->E_last} : z;
     // no table until a batch shares one among the simulations it fits
     c.sig = nullptr;
     c.sig_l0 = c.sig_inv = c.sig_tmax = 0.0f;

@@ -430,7 +430,7 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
         s2 = (T)0;
     } else {
         bool oor = false;
-        W = table_pick<T>(ch == MCD_CH_MOLLER ? c.tm : c.tg, E, Ops<T>::unit(r.z), &oor);
+        W = table_pick<T>(c.tab[ch != MCD_CH_MOLLER], E, Ops<T>::unit(r.z), &oor);
         if (oor) L.flags |= F_TABLE_RANGE;
         // binary collision (MC/tools/scattering.py:156-179)
         if (W <= (E - c.Ef) * (T)0.5) {
