@@ -148,18 +148,85 @@ def cpu_sample(sims, per_sim, steps=1, seed=0):
                                                                      s["tol_E"], s["tol_W"]))
               for kind in ("Moller", "Gryz")]
         prepared.append((mat, ht, min(per_sim, s["num_el"])))
-    times, events, electrons = [], 0, 0
+    times, events, electrons, bks, ns = [], 0, 0, [], []
     for _ in range(steps):
         t0 = time.perf_counter()
         ev = el = 0
+        bks, ns = [], []
         for k, (s, (mat, ht, n)) in enumerate(zip(sims, prepared)):
             r = coracle.run(mat, s["E0"], s["Emin"], s["s_tilt"], n, seed=seed, mode="DS", Wc=s["Wc"],
                             tables=ht, sim_id=k, nthreads=threads)
             ev += int(r["n_events"].sum())
             el += n
+            bks.append(int((r["outcome"] == 1).sum()))
+            ns.append(n)
         times.append(time.perf_counter() - t0)
         events, electrons = ev, el
-    return {"times": times, "events": events, "electrons": electrons, "threads": threads}
+    return {"times": times, "events": events, "electrons": electrons, "threads": threads, "bks": bks, "n": ns}
+
+
+CFG1_WORKLOAD = ("DS Si, E0 10 keV, Emin 1 keV, tilt 0 deg, Wc 100 eV, tol 1e-3, 1000 electrons, FP64 "
+                 "transport with per-electron rows")
+
+
+def cfg1_bench(args, dev):
+    """The small plain configuration in full on both sides: one FP64 launch
+    against the C oracle on 1 core and on all host cores (same Philox stream,
+    so the two follow the same trajectories)."""
+    import torch
+    import coracle
+    import mcd_oracle as O
+    from mcd import _lib, engine, tables
+    p = dict(material="Si", E0=10000.0, Emin=1000.0, s_tilt=0.0, Wc=100.0, tol_E=1e-3, tol_W=1e-3, mode="DS")
+    n = 1000
+    mat = _lib.material("Si")
+    dt = tables.ds_tables(mat, 10000.0, 1000.0, 100.0, 1e-3, 1e-3, dev)
+    sim = engine.make_sim(p, n, seed=args.seed, precision=_lib.FP64)
+    bufs = engine.RunBuffers(n, _lib.FP64, True, 0, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        bufs.zero()
+        engine.launch(sim, mat, dt, bufs)
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(max(3, args.steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bufs.zero()
+        e0.record(stream)
+        engine.launch(sim, mat, dt, bufs)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    g = engine.collect(bufs)
+    # the same launch in FP32 transport
+    sim32 = engine.make_sim(p, n, seed=args.seed, precision=_lib.FP32)
+    b32 = engine.RunBuffers(n, _lib.FP32, True, 0, device=dev)
+    ms32 = []
+    for k in range(args.warmup + max(3, args.steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b32.zero()
+        e0.record(stream)
+        engine.launch(sim32, mat, dt, b32)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if k >= args.warmup:
+            ms32.append(e0.elapsed_time(e1))
+    om = O.Material("Si")
+    ht = [coracle.HostTable(t.Ws.cpu().numpy(), t.Es.cpu().numpy(), t.cdf.cpu().numpy()) for t in dt]
+    cpu = {}
+    for th in (1, os.cpu_count() or 1):
+        t0 = time.perf_counter()
+        c = coracle.run(om, 10000.0, 1000.0, 0.0, n, seed=args.seed, mode="DS", Wc=100.0, tables=ht, nthreads=th)
+        cpu[th] = time.perf_counter() - t0
+    ev = int(g.tally["events"])
+    same = float(np.mean((g.electrons["outcome"] == c["outcome"]) & (g.electrons["n_events"] == c["n_events"])))
+    return {"workload": CFG1_WORKLOAD, "num_el": n, "events": ev, "gpu_ms": statistics.median(ms),
+            "gpu_events_per_s": ev / statistics.median(ms) * 1e3, "gpu_fp32_ms": statistics.median(ms32),
+            "note": "1000 electrons fill 8 blocks of 128 threads: the launch lasts as long as its longest "
+                    "trajectory, and FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU",
+            "cpu_1core_s": cpu[1], "cpu_all_cores_s": cpu[os.cpu_count() or 1], "cpu_cores": os.cpu_count() or 1,
+            "eta_gpu_fp64": g.tally["bks"] / n, "eta_oracle": float(np.mean(c["outcome"] == 1)),
+            "identical_trajectories": same, "gpu_launches": 2 * max(3, args.steps)}
 
 
 def run_reference(args):
@@ -505,6 +572,18 @@ def run_mcd(args):
     else:
         cpu = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=1, seed=args.seed)
     cpu_v = cpu["events"] / cpu["times"][0]
+    # eta of every simulation against the FP64 oracle's sample of its first electrons
+    vs_oracle = None
+    if not args.no_cpu:
+        zo = []
+        for k, t in enumerate(tallies):
+            n = sum(t[o] for o in ("bks", "abs", "trsm", "long"))
+            k2, n2 = cpu["bks"][k], cpu["n"][k]
+            pp = (t["bks"] + k2) / (n + n2)
+            zo.append(abs(t["bks"] / n - k2 / n2) / math.sqrt(max(pp * (1 - pp), 1e-12) * (1 / n + 1 / n2)))
+        vs_oracle = {"max_z": max(zo), "mean_z": sum(zo) / len(zo), "sims": len(zo),
+                     "oracle_electrons_per_sim": "min(num_el, %d)" % CPU_SAMPLE_PER_SIM}
+    c1 = None if args.no_cfg1 else cfg1_bench(args, dev)
 
     line = {
         "metric": "scatter events/s", "value": value, "unit": "events/s", "n_gpus": ws, "steps": K,
@@ -520,7 +599,7 @@ def run_mcd(args):
         "plain": {"value": plain_value, "unit": "events/s", "ms_per_step": 1e3 * t_plain / k_plain,
                   "launches_per_step": len(sims)},
         "batched_over_plain": value / plain_value,
-        "eta": {"batched_vs_plain_max_z": max(zs), "vs_reference": ref},
+        "eta": {"batched_vs_plain_max_z": max(zs), "vs_reference": ref, "vs_oracle_fp64": vs_oracle},
         "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": batch.ws_bytes,
                 "d2h_bytes_per_step": int(batch.tallies.numel())},
         "roofline": {"bound": "fp32-issue", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -534,6 +613,7 @@ def run_mcd(args):
         "adjoint": adj,
         "stream": stream,
         "cont": cont,
+        "cfg1": c1,
         "detector": det,
         "gpu_launches": K,
         "status": status,
@@ -561,6 +641,7 @@ def main():
     ap.add_argument("--no-stream", action="store_true", help="skip the streamed-event measurement")
     ap.add_argument("--no-cont", action="store_true", help="skip the continuous-mode histogram measurement")
     ap.add_argument("--no-detector", action="store_true", help="skip the detector-projection measurement")
+    ap.add_argument("--no-cfg1", action="store_true", help="skip the small FP64 configuration")
     ap.add_argument("--stream-fraction", type=float, default=1.0,
                     help="fraction of the 1e7-electron streaming workload to run (1 = all of it)")
     args = ap.parse_args()
