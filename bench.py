@@ -296,10 +296,49 @@ def adjoint_bench(args, dev):
     Lm = float(np.sum((m.chain(1 - d, 1.0)[0] - t) ** 2))
     fd = (Lp - Lm) / (2 * d)
     h, _, _ = m.forward(1.0, 1.0)     # restore the checkpoints of J = 1
+    depth = adjoint_depth_bench(args, dev, p, n)
     return {"workload": ADJ_WORKLOAD, "num_el": n, "fwd_ms": tf / args.steps, "bwd_ms": tb / args.steps,
             "bwd_over_fwd": tb / tf, "loss": L, "dL_dJscale": dJ, "dL_dnscale": dn,
             "fd_frozen_dL_dJscale": fd, "fd_frozen_rel_err": abs(dJ - fd) / abs(fd) if fd else None,
-            "fd_step": d, "gpu_launches": 2 * args.steps}
+            "fd_step": d, "max_depth": depth, "gpu_launches": 2 * args.steps + depth["gpu_launches"]}
+
+
+def adjoint_depth_bench(args, dev, p, n):
+    """The same workload with the deepest z of backscattered electrons binned
+    (64 Gaussian-soft bins over 0-20000 A, sigma 300 A; target made with
+    J x 1.1): the adjoint runs through every deflection."""
+    import torch
+    from mcd.adjoint import ExitEnergyModel
+    m = ExitEnergyModel(p, n, seed=args.seed, precision="fp32", device=dev, quantity="max_depth", lo=0.0,
+                        hi=20000.0, sigma=300.0)
+    t, _, _ = m.forward(1.1, 1.0)
+    h, _, _ = m.forward(1.0, 1.0)
+    g = 2.0 * (h - t)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        m.launch_forward(1.0, 1.0)
+        m.launch_backward(g, 0.0)
+    torch.cuda.synchronize(dev)
+    tf = tb = 0.0
+    for _ in range(args.steps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        m.launch_forward(1.0, 1.0)
+        e1.record(stream)
+        m.launch_backward(g, 0.0)
+        e2.record(stream)
+        torch.cuda.synchronize(dev)
+        tf += e0.elapsed_time(e1)
+        tb += e1.elapsed_time(e2)
+    h, _, _ = m.forward(1.0, 1.0)
+    dJ, dn = m.backward(2.0 * (h - t), 0.0)
+    d = 1e-3
+    fdJ = (float(np.sum((m.chain(1 + d, 1.0)[0] - t) ** 2)) - float(np.sum((m.chain(1 - d, 1.0)[0] - t) ** 2))) / (2 * d)
+    fdn = (float(np.sum((m.chain(1.0, 1 + d)[0] - t) ** 2)) - float(np.sum((m.chain(1.0, 1 - d)[0] - t) ** 2))) / (2 * d)
+    return {"fwd_ms": tf / args.steps, "bwd_ms": tb / args.steps, "bwd_over_fwd": tb / tf,
+            "dL_dJscale": dJ, "dL_dnscale": dn, "fd_frozen_rel_err_J": abs(dJ - fdJ) / abs(fdJ) if fdJ else None,
+            "fd_frozen_rel_err_n": abs(dn - fdn) / abs(fdn) if fdn else None, "fd_step": d,
+            "gpu_launches": 2 * args.steps}
 
 
 CONT_WORKLOAD = ("continuous JL Bethe, Cu, E0 20 keV, Emin 1 keV, tilt 70 deg, 1e6 electrons, FP32; "

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 4
+#define MCD_ABI_VERSION 5
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -285,24 +285,31 @@ int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* tallies,
 /* Gaussian-soft exit-energy histogram of backscattered electrons:
  * h_b = (1/num_el) sum exp(-(E_exit - c_b)^2 / (2 sigma^2)),
  * c_b = lo + (b + 1/2) (hi - lo) / nbins.                                    */
+enum { MCD_ADJ_EXIT_E = 0,      /* exit energy of 'bks' electrons, eV        */
+       MCD_ADJ_MAX_DEPTH = 1    /* deepest z reached by 'bks' electrons, A   */ };
 typedef struct mcd_softhist {
     int32_t nbins;           /* <= MCD_HIST_E_MAX                             */
-    int32_t reserved;
-    double lo, hi, sigma;    /* eV                                            */
+    int32_t quantity;        /* MCD_ADJ_*: what is binned                     */
+    double lo, hi, sigma;    /* in the quantity's unit                        */
 } mcd_softhist;
 
 /* Per-electron adjoint state (device, caller-owned).                         */
 typedef struct mcd_adjoint_buf {
-    void* ckpt;              /* T [max_ckpt][num_el]: E every 64 events       */
-    int32_t* kstar;          /* [num_el]: exit event of 'bks' electrons or -1 */
-    void* E_exit;            /* T [num_el]: energy of the first outcome row   */
+    void* ckpt;              /* T [max_ckpt][num_el] (exit energy: E every 64
+                                events) or T [max_ckpt][8][num_el] (depth: E,
+                                z, direction and local y axis every 64 events) */
+    int32_t* kstar;          /* [num_el], 'bks' electrons, else -1: the exit
+                                event (exit energy) or the number of events
+                                up to the deepest point (depth)              */
+    void* E_exit;            /* T [num_el]: the binned quantity (exit energy
+                                of the first outcome row, or deepest z)     */
     int32_t max_ckpt;
     int32_t reserved;
 } mcd_adjoint_buf;
 
 /* Continuous-mode forward pass that also stores the adjoint checkpoints.
  * hist_out[nbins + 2] (device, zeroed by the caller) receives the unnormalised
- * soft bins, the sum of exit energies and the number of 'bks' electrons; tally
+ * soft bins of hist->quantity, its sum and the number of 'bks' electrons; tally
  * (may be NULL) the outcome and event counts.  sim->J_scale and sim->n_scale
  * scale the Bethe J and the density.  Replaces multiTraj_cont + trajectory_cont_cl
  * (MC/tools/multiScatter.py:171-229, MC/tools/singleScatter.py:205-239) with
@@ -311,17 +318,19 @@ int mcd_adjoint_forward(const mcd_sim* sim, const mcd_material* mat, const mcd_s
                         const mcd_adjoint_buf* buf, double* hist_out, mcd_tally* tally,
                         uint32_t* status, void* stream);
 
-/* Reverse sweep: grad_hist[nbins + 1] holds dL/dh_b and dL/d(sum of exit
- * energies); grad[2] (device, zeroed by the caller) receives dL/dJ_scale and
+/* Reverse sweep: grad_hist[nbins + 1] holds dL/dh_b and dL/d(sum of the
+ * quantity); grad[2] (device, zeroed by the caller) receives dL/dJ_scale and
  * dL/dn_scale, the pathwise derivatives with random numbers and event
- * sequence frozen.  Each 64-event segment is recomputed from its checkpoint
- * and the Philox counters.  No counterpart in the reference.                 */
+ * sequence (for depth also the deepest event) frozen.  Each 64-event segment
+ * is recomputed from its checkpoint and the Philox counters; for depth the
+ * sweep carries the adjoints of the energy, the direction and the local y
+ * axis through the Rutherford deflections.  No counterpart in the reference. */
 int mcd_adjoint(const mcd_sim* sim, const mcd_material* mat, const mcd_softhist* hist,
                 const mcd_adjoint_buf* buf, const double* grad_hist, double* grad, void* stream);
 
-/* The exit energies along the frozen event sequence of the last forward pass,
- * at this call's J_scale / n_scale, as soft bins (for finite-difference checks
- * of mcd_adjoint).  No counterpart in the reference.                        */
+/* The binned quantity along the frozen event sequence of the last forward
+ * pass, at this call's J_scale / n_scale, as soft bins (for finite-difference
+ * checks of mcd_adjoint).  No counterpart in the reference.                  */
 int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_softhist* hist,
                       const mcd_adjoint_buf* buf, double* hist_out, void* stream);
 

@@ -38,8 +38,11 @@ struct AdjBuf {
 
 struct SoftHist {
     int32_t nbins;
+    int32_t quantity;   // MCD_ADJ_EXIT_E or MCD_ADJ_MAX_DEPTH
     double lo, width, inv2s2, inv_s2;
 };
+
+constexpr int kDepthState = 8;   // E, z, d (3), y (3) per depth checkpoint
 
 // Gaussian soft bins within 8 sigma of E: calls f(bin, weight, d = E - c_b)
 template <class F>
@@ -100,27 +103,49 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t st = 0;
     if (i < (uint64_t)c.num_el) {
+        const bool depth = sh.quantity == MCD_ADJ_MAX_DEPTH;
         Lane<T> L;
         lane_init(L, c);
         const uint64_t elec = c.first + i;
         T* ck = static_cast<T*>(buf.ckpt);
         const size_t n = (size_t)c.num_el;
-        int kstar = -1;
+        int kstar = -1, mstar = 0;   // exit event; events up to the deepest point
+        T zbest = (T)0;
         while (L.outcome == MCD_OUT_NONE) {
             if ((L.step % kSeg) == 0) {
                 const int64_t m = L.step / kSeg;
-                if (m < buf.max_ckpt) ck[(size_t)m * n + i] = L.E;
+                if (m < buf.max_ckpt) {
+                    if (!depth) {
+                        ck[(size_t)m * n + i] = L.E;
+                    } else {
+                        T* q = ck + (size_t)m * kDepthState * n + i;
+                        q[0] = L.E;
+                        q[n] = L.z;
+                        q[2 * n] = L.dx;
+                        q[3 * n] = L.dy;
+                        q[4 * n] = L.dz;
+                        q[5 * n] = L.yx;
+                        q[6 * n] = L.yy;
+                        q[7 * n] = L.yz;
+                    }
+                }
             }
             EventOut<T> ev;
             cont_event<T, false>(L, c, elec, &ev);
             if (L.outcome == MCD_OUT_BKS) kstar = (int)(L.step - 1);
+            if (L.max_z > zbest) {
+                zbest = L.max_z;
+                mstar = (int)L.step;
+            }
         }
         const bool bks = L.outcome == MCD_OUT_BKS;
-        if (bks && kstar > 0 && (kstar - 1) / kSeg >= buf.max_ckpt) st |= MCD_FLAG_CKPT;
-        buf.kstar[i] = bks ? kstar : -1;
-        static_cast<T*>(buf.E_exit)[i] = L.E_row;
+        const int key = depth ? mstar : kstar;
+        if (bks && key > 0 && (key - 1) / kSeg >= buf.max_ckpt) st |= MCD_FLAG_CKPT;
+        buf.kstar[i] = bks ? key : -1;
+        const T q = depth ? L.max_z : L.E_row;
+        static_cast<T*>(buf.E_exit)[i] = q;
         if (bks) {
-            const double E = (double)L.E_row;
+            const double E = (double)q;
             soft_bins(sh, E, [&](int b, double w, double) { if (w > 0.0) atomicAdd(&sh_h[b], w); });
             atomicAdd(&sh_h[sh.nbins], E);
             atomicAdd(&sh_h[sh.nbins + 1], 1.0);
@@ -142,7 +167,110 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
     }
 }
 
-template <class T>
+// Reverse sweep of the deepest depth Z = z_{m*} = sum_{k < m*} s_k d_z,k
+// along the frozen sequence.  Per event k, with the step s(E), the energy
+// update E' = E - s S(E), the Rutherford sin^2(theta/2) = s2(E) and the
+// rotation of the frame (d, y, x = y cross d)
+//     d' = d cos(theta) + x sin(theta) cos(phi) + y sin(theta) sin(phi)
+//     y' = y cos(phi) - x sin(phi)
+// the adjoints of (E, d, y) run backwards from zero at m* (Z does not
+// depend on the state after m*), g = dL/dZ feeds the z term of every event:
+//     lE  = lE' (1 + s dlnsig S - s dS/dE) - g d_z s dlnsig
+//           + lD' . (-2 ds2/dE d + dsin(theta)/dE (x cos(phi) + y sin(phi)))
+//     lD  = cos(theta) lD' + w cross y + g s e_z
+//     lY  = sin(theta) sin(phi) lD' + cos(phi) lY' + d cross w,
+//           w = sin(theta) cos(phi) lD' - sin(phi) lY'
+//     dL/dJ += lE' (-s dS/dJ);  dL/dn += g d_z (-s / n)  (E' does not depend on n)
+// (the renormalisation of d and y after each rotation is left out: it moves
+// a unit vector by rounding only).  Each segment is recomputed from its
+// checkpoint with the forward's own event code.
+template <class T, class C>
+__device__ __forceinline__ void depth_sweep(const C& c, const AdjBuf& buf, uint64_t i, uint64_t elec, int mstar,
+                                            T g, T ij, T ins, T* gj, T* gn) {
+    const T* ck = static_cast<const T*>(buf.ckpt);
+    const size_t n = (size_t)c.num_el;
+    T lE = (T)0, ldx = (T)0, ldy = (T)0, ldz = (T)0, lyx = (T)0, lyy = (T)0, lyz = (T)0;
+    T sj = (T)0, sn = (T)0;
+    T aE[kSeg], aS[kSeg], aS2[kSeg], aU[kSeg], aP[kSeg], aD[3][kSeg], aY[3][kSeg];
+    for (int m = (mstar - 1) / kSeg; m >= 0; --m) {
+        const int k0 = m * kSeg;
+        const int len = min(kSeg, mstar - k0);
+        const T* q = ck + (size_t)m * kDepthState * n + i;
+        Lane<T> L;
+        lane_init(L, c);
+        L.E = q[0];
+        L.z = q[n];
+        L.dx = q[2 * n];
+        L.dy = q[3 * n];
+        L.dz = q[4 * n];
+        L.yx = q[5 * n];
+        L.yy = q[6 * n];
+        L.yz = q[7 * n];
+        L.step = k0;
+        for (int j = 0; j < len; ++j) {   // the forward's events, recorded
+            aE[j] = L.E;
+            aD[0][j] = L.dx;
+            aD[1][j] = L.dy;
+            aD[2][j] = L.dz;
+            aY[0][j] = L.yx;
+            aY[1][j] = L.yy;
+            aY[2][j] = L.yz;
+            EventOut<T> ev;
+            cont_event<T, true>(L, c, elec, &ev);
+            aS[j] = ev.pathl;
+            aS2[j] = ev.s2;
+            aU[j] = ev.u_ang;
+            aP[j] = ev.u_phi;
+        }
+        for (int j = len - 1; j >= 0; --j) {   // reverse sweep
+            const T E = aE[j], s = aS[j], s2 = aS2[j];
+            const T dx = aD[0][j], dy = aD[1][j], dz = aD[2][j];
+            const T yx = aY[0][j], yy = aY[1][j], yz = aY[2][j];
+            T S, SE, Sj;
+            stopping_derivs<T>(c, E, &S, &SE, &Sj);
+            const T dl = dlnsig<T>(c, E);
+            // angles of the event
+            T sp, cp;
+            Ops<T>::sincos_pi(aP[j], &sp, &cp);
+            if (c.quirks & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
+            const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
+            const T cth = (T)1 - (T)2 * s2;
+            const T sth = (T)2 * Ops<T>::sqrt_(s2) * Ops<T>::sqrt_((T)1 - s2);
+            // d s2 / dE with s2 = a U / (a + 1 - U), a = a0 / E
+            const T a = Ops<T>::div(c.a0, E), U = aU[j], Uc = (T)1 - U;
+            const T den = a + Uc;
+            const T ds2 = -Ops<T>::div(a, E) * Ops<T>::div(U * Uc, den * den);
+            const T dsth = sth > (T)0 ? Ops<T>::div((T)2 * cth * ds2, sth) : (T)0;
+            const T xx = yy * dz - yz * dy, xy = yz * dx - yx * dz, xz = yx * dy - yy * dx;
+            const T sa = sth * cph, sb = sth * sph;
+            // parameter gradients use the adjoint of the event's outputs
+            sj += lE * (-s * Sj * ij);
+            sn += g * dz * (-s * ins);
+            const T rot = ldx * (-(T)2 * ds2 * dx + dsth * (cph * xx + sph * yx)) +
+                          ldy * (-(T)2 * ds2 * dy + dsth * (cph * xy + sph * yy)) +
+                          ldz * (-(T)2 * ds2 * dz + dsth * (cph * xz + sph * yz));
+            const T nE = lE * ((T)1 + s * dl * S - s * SE) - g * dz * s * dl + rot;
+            const T wx = sa * ldx - sph * lyx, wy = sa * ldy - sph * lyy, wz = sa * ldz - sph * lyz;
+            const T ndx = cth * ldx + (wy * yz - wz * yy);
+            const T ndy = cth * ldy + (wz * yx - wx * yz);
+            const T ndz = cth * ldz + (wx * yy - wy * yx) + g * s;
+            const T nyx = sb * ldx + cph * lyx + (dy * wz - dz * wy);
+            const T nyy = sb * ldy + cph * lyy + (dz * wx - dx * wz);
+            const T nyz = sb * ldz + cph * lyz + (dx * wy - dy * wx);
+            lE = nE;
+            ldx = ndx;
+            ldy = ndy;
+            ldz = ndz;
+            lyx = nyx;
+            lyy = nyy;
+            lyz = nyz;
+        }
+    }
+    *gj = sj;
+    *gn = sn;
+}
+
+template <class T, bool DEPTH>
 __global__ void __launch_bounds__(128) k_adj_bwd(const SimConst<T> cp, const SoftHist sh, const AdjBuf buf,
                                                  const double* grad_h, double inv_n, double inv_j,
                                                  double inv_ns, double* grad) {
@@ -155,7 +283,18 @@ __global__ void __launch_bounds__(128) k_adj_bwd(const SimConst<T> cp, const Sof
     __syncthreads();
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double gj = 0.0, gn = 0.0;
-    if (i < (uint64_t)c.num_el) {
+    if (DEPTH && i < (uint64_t)c.num_el) {
+        const int mstar = buf.kstar[i];
+        if (mstar > 0 && (mstar - 1) / kSeg < buf.max_ckpt) {
+            const double Z = (double)static_cast<const T*>(buf.E_exit)[i];
+            double g0 = grad_h[sh.nbins];
+            soft_bins(sh, Z, [&](int b, double w, double d) { g0 += grad_h[b] * inv_n * (-d * sh.inv_s2) * w; });
+            T sj, sn;
+            depth_sweep<T>(c, buf, i, c.first + i, mstar, (T)g0, (T)inv_j, (T)inv_ns, &sj, &sn);
+            gj = (double)sj;
+            gn = (double)sn;
+        }
+    } else if (!DEPTH && i < (uint64_t)c.num_el) {
         const int kstar = buf.kstar[i];
         if (kstar > 0 && (kstar - 1) / kSeg < buf.max_ckpt) {
             const T* ck = static_cast<const T*>(buf.ckpt);
@@ -224,12 +363,24 @@ __global__ void __launch_bounds__(256) k_adj_chain(const SimConst<T> cp, const S
         const int kstar = buf.kstar[i];
         if (kstar >= 0) {
             const uint64_t elec = c.first + i;
-            T E = c.E0;
-            for (int k = 0; k < kstar; ++k) {
-                const T s = step_len<T>(c, E, elec, k);
-                E = E - Ops<T>::mul_rn(s, stopping<T>(c, E));
+            double Ed;
+            if (sh.quantity == MCD_ADJ_MAX_DEPTH) {
+                // the forward's own events up to the deepest point
+                Lane<T> L;
+                lane_init(L, c);
+                for (int k = 0; k < kstar; ++k) {
+                    EventOut<T> ev;
+                    cont_event<T, false>(L, c, elec, &ev);
+                }
+                Ed = (double)L.z;
+            } else {
+                T E = c.E0;
+                for (int k = 0; k < kstar; ++k) {
+                    const T s = step_len<T>(c, E, elec, k);
+                    E = E - Ops<T>::mul_rn(s, stopping<T>(c, E));
+                }
+                Ed = (double)E;
             }
-            const double Ed = (double)E;
             soft_bins(sh, Ed, [&](int b, double w, double) { if (w > 0.0) atomicAdd(&sh_h[b], w); });
             atomicAdd(&sh_h[sh.nbins], Ed);
             atomicAdd(&sh_h[sh.nbins + 1], 1.0);
@@ -249,8 +400,10 @@ static int adj_args(const mcd_sim* sim, const mcd_material* mat, const mcd_softh
     if (hist->nbins < 1 || hist->nbins > MCD_HIST_E_MAX) return MCD_ETOOBIG;
     if (!(hist->sigma > 0) || !(hist->hi > hist->lo)) return MCD_EINVAL;
     if (!buf->ckpt || !buf->kstar || !buf->E_exit || buf->max_ckpt < 1) return MCD_EINVAL;
+    if (hist->quantity != MCD_ADJ_EXIT_E && hist->quantity != MCD_ADJ_MAX_DEPTH) return MCD_EINVAL;
     if (!(sim->J_scale >= 0) || !(sim->n_scale >= 0)) return MCD_EINVAL;
     sh->nbins = hist->nbins;
+    sh->quantity = hist->quantity;
     sh->lo = hist->lo;
     sh->width = (hist->hi - hist->lo) / hist->nbins;
     sh->inv2s2 = 1.0 / (2.0 * hist->sigma * hist->sigma);
@@ -301,12 +454,20 @@ extern "C" int mcd_adjoint(const mcd_sim* sim, const mcd_material* mat, const mc
     const double js = 1.0 / (sim->J_scale > 0 ? sim->J_scale : 1.0);
     const double ns = 1.0 / (sim->n_scale > 0 ? sim->n_scale : 1.0);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (sim->precision == MCD_FP64)
-        k_adj_bwd<double><<<(unsigned)grid, 128, 0, st>>>(make_consts<double>(*sim, *mat, nullptr, nullptr), sh, ab,
-                                                           grad_hist, inv_n, js, ns, grad);
-    else
-        k_adj_bwd<float><<<(unsigned)grid, 128, 0, st>>>(make_consts<float>(*sim, *mat, nullptr, nullptr), sh, ab,
-                                                          grad_hist, inv_n, js, ns, grad);
+    const bool depth = sh.quantity == MCD_ADJ_MAX_DEPTH;
+    if (sim->precision == MCD_FP64) {
+        const SimConst<double> c = make_consts<double>(*sim, *mat, nullptr, nullptr);
+        if (depth)
+            k_adj_bwd<double, true><<<(unsigned)grid, 128, 0, st>>>(c, sh, ab, grad_hist, inv_n, js, ns, grad);
+        else
+            k_adj_bwd<double, false><<<(unsigned)grid, 128, 0, st>>>(c, sh, ab, grad_hist, inv_n, js, ns, grad);
+    } else {
+        const SimConst<float> c = make_consts<float>(*sim, *mat, nullptr, nullptr);
+        if (depth)
+            k_adj_bwd<float, true><<<(unsigned)grid, 128, 0, st>>>(c, sh, ab, grad_hist, inv_n, js, ns, grad);
+        else
+            k_adj_bwd<float, false><<<(unsigned)grid, 128, 0, st>>>(c, sh, ab, grad_hist, inv_n, js, ns, grad);
+    }
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 

@@ -234,6 +234,7 @@ template <class T>
 struct EventOut {
     T E, W, pathl, c2, half_phi, x, y, z;
     int ch;
+    T s2, u_ang, u_phi;   // sin^2(theta/2) and the uniforms of the angles (adjoint)
 };
 
 // Position update and the exit tests (MC/tools/electron.py:64-84): leaving
@@ -495,6 +496,9 @@ __device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec,
     const T s2 = Ops<T>::div(a * Ops<T>::unit(r.z), a + Ops<T>::unit_c(r.z));
     const T uphi = Ops<T>::unit(r.w);
     if (REC) {
+        ev->s2 = s2;
+        ev->u_ang = Ops<T>::unit(r.z);
+        ev->u_phi = uphi;
         ev->E = E;
         ev->W = dE;
         ev->pathl = s;

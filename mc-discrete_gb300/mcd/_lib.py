@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 MAX_SHELLS = 8
 GUIDE = 256
 MAX_CHANNELS = 16
@@ -35,6 +35,7 @@ ELASTIC = {"Ruth_vanilla": ELASTIC_RUTH, "Ruth_vanilla_wDefl": ELASTIC_RUTH_WDEF
 MODE_DS, MODE_CONT = 0, 1
 BETHE = {"classical": 0, "JL": 1, "explicit": 2}
 FP32, FP64 = 0, 1
+ADJ_EXIT_E, ADJ_MAX_DEPTH = 0, 1
 TABLE_MOLLER, TABLE_GRYZ = 0, 1
 
 Q_CROSSING_STEP = 0x1
@@ -173,7 +174,7 @@ class Tune(C.Structure):
 
 
 class SoftHist(C.Structure):
-    _fields_ = [("nbins", C.c_int32), ("reserved", C.c_int32), ("lo", C.c_double), ("hi", C.c_double),
+    _fields_ = [("nbins", C.c_int32), ("quantity", C.c_int32), ("lo", C.c_double), ("hi", C.c_double),
                 ("sigma", C.c_double)]
 
 

@@ -1,17 +1,20 @@
 """Differentiable continuous-mode transport.
 
 ExitEnergyModel runs the continuous-slowing-down transport (mcd_adjoint_forward)
-and keeps, per electron, the energy every 64 events and the event in which it
-left through the surface.  Its backward pass (mcd_adjoint) recomputes each
-64-event segment from the Philox counters and sweeps the energy recursion
-E_{k+1} = E_k - s_k S(E_k) in reverse, giving the pathwise derivatives of
+and keeps, per electron, checkpoints every 64 events.  Its backward pass
+(mcd_adjoint) recomputes each 64-event segment from the Philox counters and
+sweeps it in reverse, giving the pathwise derivatives of
 
-    h_b = (1/N) sum_{bks} exp(-(E_exit - c_b)^2 / (2 sigma^2))   (b < nbins)
-    m   = mean exit energy of backscattered electrons
+    h_b = (1/N) sum_{bks} exp(-(q - c_b)^2 / (2 sigma^2))   (b < nbins)
+    m   = mean of q over backscattered electrons
 
-with respect to the Bethe mean ionisation energy J and the density, both as
-multipliers of the reference values (J_scale, n_scale), with the random
-numbers and the event sequence frozen.
+for q the exit energy (quantity="exit_E": the energy recursion
+E_{k+1} = E_k - s_k S(E_k) alone) or the deepest z reached
+(quantity="max_depth": energy, direction and local frame through every
+Rutherford deflection up to the deepest point), with respect to the Bethe
+mean ionisation energy J and the density, both as multipliers of the
+reference values (J_scale, n_scale), with the random numbers and the event
+sequence frozen.
 
 ExitHistogram.apply(J_scale, n_scale, model) wraps it as a torch.autograd
 Function.
@@ -33,7 +36,7 @@ class ExitEnergyModel:
     """One continuous-mode simulation whose exit-energy tallies are differentiable."""
 
     def __init__(self, input_par, num_el, seed=0, nbins=64, sigma=50.0, lo=None, hi=None, precision="fp32",
-                 max_ckpt=64, device="cuda"):
+                 max_ckpt=64, device="cuda", quantity="exit_E"):
         torch = _torch()
         self.p = with_defaults(input_par)
         if "DS" in self.p["mode"]:
@@ -43,9 +46,14 @@ class ExitEnergyModel:
         self.prec = _lib.FP64 if precision in ("fp64", _lib.FP64) else _lib.FP32
         self.device = torch.device(device)
         self.mat = _lib.material(self.p["material"])
+        if quantity not in ("exit_E", "max_depth"):
+            raise ValueError("quantity is 'exit_E' or 'max_depth'")
+        self.depth = quantity == "max_depth"
+        if self.depth and (lo is None or hi is None):
+            raise ValueError("a depth histogram needs lo and hi (A)")
         lo = float(self.p["Emin"]) if lo is None else float(lo)
         hi = float(self.p["E0"]) if hi is None else float(hi)
-        self.hist = SoftHist(int(nbins), 0, lo, hi, float(sigma))
+        self.hist = SoftHist(int(nbins), _lib.ADJ_MAX_DEPTH if self.depth else _lib.ADJ_EXIT_E, lo, hi, float(sigma))
         self.nbins = int(nbins)
         self.max_ckpt = int(max_ckpt)
         self._alloc()
@@ -54,7 +62,8 @@ class ExitEnergyModel:
     def _alloc(self):
         torch = _torch()
         dt = torch.float32 if self.prec == _lib.FP32 else torch.float64
-        self.ckpt = torch.empty((self.max_ckpt, self.n), dtype=dt, device=self.device)
+        shape = (self.max_ckpt, 8, self.n) if self.depth else (self.max_ckpt, self.n)
+        self.ckpt = torch.empty(shape, dtype=dt, device=self.device)
         self.kstar = torch.empty(self.n, dtype=torch.int32, device=self.device)
         self.E_exit = torch.empty(self.n, dtype=dt, device=self.device)
         self.buf = AdjointBuf(self.ckpt.data_ptr(), self.kstar.data_ptr(), self.E_exit.data_ptr(), self.max_ckpt, 0)

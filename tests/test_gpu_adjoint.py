@@ -98,3 +98,49 @@ def test_autograd_function_matches_model():
     assert abs(float(J.grad) - dJ) <= 1e-12 * abs(dJ)
     assert abs(float(n.grad) - dn) <= 1e-9 * abs(dJ)
     assert 1000.0 < float(mean) < 15000.0
+
+
+# deepest z of backscattered electrons, 64 soft bins of 0-20000 A (sigma 300 A):
+# the adjoint runs through the energy, the direction and the local frame
+DEPTH = dict(quantity="max_depth", lo=0.0, hi=20000.0, sigma=300.0)
+
+
+def test_fp64_depth_adjoint_equals_frozen_fd():
+    m = ExitEnergyModel(AL, 20000, seed=13, precision="fp64", **DEPTH)
+    t, _, _ = m.forward(1.1, 1.1)
+    L, dJ, dn = loss_grad(m, t)
+    assert L > 0
+    d = 1e-5
+    fdJ = (chain_loss(m, t, 1 + d) - chain_loss(m, t, 1 - d)) / (2 * d)
+    fdn = (chain_loss(m, t, 1.0, 1 + d) - chain_loss(m, t, 1.0, 1 - d)) / (2 * d)
+    assert abs(dJ - fdJ) <= 1e-5 * abs(fdJ), (dJ, fdJ)
+    assert abs(dn - fdn) <= 1e-5 * abs(fdn), (dn, fdn)
+    # unlike the exit energy, the depth scales with the density (steps ~ 1/n)
+    assert abs(dn) > 0.1 * abs(dJ)
+
+
+def test_fp32_depth_adjoint_against_fd_and_fp64():
+    m32 = ExitEnergyModel(AL, 50000, seed=17, precision="fp32", **DEPTH)
+    m64 = ExitEnergyModel(AL, 50000, seed=17, precision="fp64", **DEPTH)
+    t, _, _ = m64.forward(1.1, 1.1)
+    _, dJ32, dn32 = loss_grad(m32, t)
+    _, dJ64, dn64 = loss_grad(m64, t)
+    d = 1e-3
+    fdJ = (chain_loss(m32, t, 1 + d) - chain_loss(m32, t, 1 - d)) / (2 * d)
+    fdn = (chain_loss(m32, t, 1.0, 1 + d) - chain_loss(m32, t, 1.0, 1 - d)) / (2 * d)
+    assert abs(dJ32 - fdJ) <= 2e-3 * abs(fdJ), (dJ32, fdJ)
+    assert abs(dn32 - fdn) <= 2e-3 * abs(fdn), (dn32, fdn)
+    assert abs(dJ32 - dJ64) <= 3e-2 * abs(dJ64), (dJ32, dJ64)
+    assert abs(dn32 - dn64) <= 3e-2 * abs(dn64), (dn32, dn64)
+
+
+def test_depth_chain_reproduces_forward():
+    """At the forward's own parameters the frozen-sequence recomputation gives
+    the forward's depths (it runs the same event code; the bins are sums of
+    atomic additions, so their order, and the last bits, may differ)."""
+    m = ExitEnergyModel(AL, 5000, seed=19, precision="fp32", **DEPTH)
+    h, s, nb = m.forward(1.0, 1.0)
+    hc, sc, nbc = m.chain(1.0, 1.0)
+    assert nb == nbc
+    assert abs(s - sc) <= 1e-12 * abs(s)
+    assert np.allclose(h, hc, rtol=1e-12, atol=0.0)
