@@ -97,8 +97,9 @@ struct SimConst {
     // cumulative channel cross sections tabulated on a log-E grid (batched
     // kernel only; nullptr = evaluate inline).  Row i (of sig_rows, sig_S
     // floats apart) holds, at E = 2^(sig_l0 + i / sig_inv), E times the
-    // running sums over the channels in pick order: Ruth, Moller,
-    // Gryz[0..nsh-1], Quinn (sig_K = nsh + 3 columns; padding FLT_MAX).
+    // total, then E times the running sums over the channels in pick order
+    // before the last: Ruth, Moller, Gryz[0..nsh-1] (sig_K = nsh + 3 columns;
+    // padding FLT_MAX).  The total and the first sums share one 16-byte load.
     // E * sigma varies slowly in log E, so linear interpolation at 128 rows
     // per octave is within 3e-7 of the exact sums (relative to the total).
     const float* sig;

@@ -328,17 +328,20 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     const float* r0 = c.sig + i * S;
     const float* r1 = r0 + S;
     const int K = c.sig_K;
-    const float a = __ldg(r0 + K - 1), b = __ldg(r1 + K - 1);
-    const float tot = fmaf(f, b - a, a);
+    // column 0 holds the total, columns 1.. the running sums before it
+    const float4 x0 = __ldg(reinterpret_cast<const float4*>(r0));
+    const float4 y0 = __ldg(reinterpret_cast<const float4*>(r1));
+    const float tot = fmaf(f, y0.x - x0.x, x0.x);
     const float all = fmaf(E, c.dS, tot);   // + diffraction (dS = 0 when off)
     *Etot_out = all;
     const float target = U * all;
     if (c.diff && target > tot) return MCD_CH_DIFF;
     // the running sums increase along the row (padding holds FLT_MAX), so
-    // the first column >= target is the number of columns below it
-    int j = 0;
+    // the channel is the number of them below the target
+    int j = (fmaf(f, y0.y - x0.y, x0.y) < target) + (fmaf(f, y0.z - x0.z, x0.z) < target) +
+            (fmaf(f, y0.w - x0.w, x0.w) < target);
 #pragma unroll
-    for (int q = 0; q < kSigStride / 4; ++q) {
+    for (int q = 1; q < kSigStride / 4; ++q) {
         if (4 * q < S) {
             const float4 x = __ldg(reinterpret_cast<const float4*>(r0) + q);
             const float4 y = __ldg(reinterpret_cast<const float4*>(r1) + q);

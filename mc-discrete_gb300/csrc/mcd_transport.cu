@@ -347,8 +347,10 @@ __global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
     float* row = reinterpret_cast<float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s) + (size_t)i * cf.sig_S;
     const double E = exp2((double)cf.sig_l0 + (double)i / (double)cf.sig_inv);
     const double invE = 1.0 / E;
+    // [E total, E running sums Ruth, +Moller, +Gryz[k] ... (the sum through
+    // Quinn is the total)], padding FLT_MAX: never below a target
     double cum = sig_ruth<double>(c, E);
-    int col = 0;
+    int col = 1;
     row[col++] = (float)(E * cum);
     cum += sig_moller<double>(c, E, invE);
     row[col++] = (float)(E * cum);
@@ -357,8 +359,8 @@ __global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
         row[col++] = (float)(E * cum);
     }
     cum += sig_quinn<double>(c, E, invE);
-    row[col++] = (float)(E * cum);
-    for (; col < cf.sig_S; ++col) row[col] = 3.402823466e38f;   // padding: never below a target
+    row[0] = (float)(E * cum);
+    for (; col < cf.sig_S; ++col) row[col] = 3.402823466e38f;
 }
 
 // Do two simulations have the same channel cross sections at every energy?
