@@ -105,7 +105,17 @@ struct SimConst {
     const float* sig;
     float sig_l0, sig_inv, sig_tmax;
     int32_t sig_K, sig_S, sig_rows;
+    // the small fields the event code tests, packed so that one load serves
+    // them all: quirks (bits 0-2, the MCD_Q_* masks), kBit* flags, sig_K
+    // (bits 8-11) and sig_S (bits 12-16)
+    uint32_t bits;
 };
+
+constexpr uint32_t kBitDiff = 1u << 3, kBitCont = 1u << 4, kBitChan = 1u << 5, kBitR2 = 1u << 6;
+template <class C>
+__host__ __device__ __forceinline__ int bits_K(const C& c) { return (int)((c.bits >> 8) & 15u); }
+template <class C>
+__host__ __device__ __forceinline__ int bits_S(const C& c) { return (int)((c.bits >> 12) & 31u); }
 
 constexpr int kSigRowsMax = 4096;      // grid points of a cross-section table, at most
 constexpr int kSigStride = 12;         // floats per row, at most (3 + MCD_MAX_SHELLS + 1)
@@ -204,6 +214,9 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     c.sig_K = m.n_shells + 3;
     c.sig_S = (c.sig_K + 3) & ~3;
     c.sig_rows = 0;
+    c.bits = (c.quirks & 7u) | (c.diff ? kBitDiff : 0u) | (c.mode == MCD_MODE_CONT ? kBitCont : 0u) |
+             ((c.tally_flags & MCD_TALLY_CHANNELS) ? kBitChan : 0u) | (c.ruth_r2 ? kBitR2 : 0u) |
+             ((uint32_t)c.sig_K << 8) | ((uint32_t)c.sig_S << 12);
     return c;
 }
 

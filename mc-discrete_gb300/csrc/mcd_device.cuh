@@ -92,7 +92,7 @@ struct Ops<double> {
 template <class T, class C>
 __device__ __forceinline__ T sig_ruth(const C& c, T E) {
     T f = c.cRs;
-    if (c.ruth_r2) {
+    if (c.bits & kBitR2) {
         const T r = Ops<T>::div(E + (T)511000, E + (T)1024000);
         f = c.cRs * r * r;
     }
@@ -287,7 +287,7 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_ph
     const T ct = Ops<T>::sqrt_((T)1 - s2);
     T sp, cp;
     Ops<T>::sincos_pi(u_phi, &sp, &cp);
-    if (c.quirks & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
+    if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
     const T cth = (T)1 - (T)2 * s2, sth = (T)2 * st * ct;
     const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
     const T xx = L.yy * L.dz - L.yz * L.dy;
@@ -324,10 +324,10 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     t = fminf(fmaxf(t, 0.0f), c.sig_tmax);
     const int i = (int)t;
     const float f = t - (float)i;
-    const int S = c.sig_S;
+    const int S = bits_S(c);
     const float* r0 = c.sig + i * S;
     const float* r1 = r0 + S;
-    const int K = c.sig_K;
+    const int K = bits_K(c);
     // column 0 holds the total, columns 1.. the running sums before it
     const float4 x0 = __ldg(reinterpret_cast<const float4*>(r0));
     const float4 y0 = __ldg(reinterpret_cast<const float4*>(r1));
@@ -335,7 +335,7 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     const float all = fmaf(E, c.dS, tot);   // + diffraction (dS = 0 when off)
     *Etot_out = all;
     const float target = U * all;
-    if (c.diff && target > tot) return MCD_CH_DIFF;
+    if ((c.bits & kBitDiff) && target > tot) return MCD_CH_DIFF;
     // the running sums increase along the row (padding holds FLT_MAX), so
     // the channel is the number of them below the target
     int j = (fmaf(f, y0.y - x0.y, x0.y) < target) + (fmaf(f, y0.z - x0.z, x0.z) < target) +
@@ -391,7 +391,7 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
         const T sQ = sig_quinn<T>(c, E, invE);
         tot += sQ;
         const T cumQ = tot;
-        if (c.diff) tot += c.dS;
+        if (c.bits & kBitDiff) tot += c.dS;
         // --- channel (MC/tools/scattering.py:39-59)
         const T target = Ops<T>::unit(r.x) * tot;
         T cum = sR;
@@ -407,7 +407,7 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
                     cum += sG[k];
                     if (ch == MCD_CH_QUINN && k < c.nsh && target <= cum) ch = MCD_CH_GRYZ0 + k;
                 }
-                if (c.diff && ch == MCD_CH_QUINN && target > cumQ) ch = MCD_CH_DIFF;
+                if ((c.bits & kBitDiff) && ch == MCD_CH_QUINN && target > cumQ) ch = MCD_CH_DIFF;
             }
         }
         inv_tot = Ops<T>::div((T)1, tot);
@@ -443,7 +443,7 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
         } else {
             L.flags |= F_NAN;
             L.nan_n += 1;
-            s2 = (c.quirks & MCD_Q_NAN_DIRECTION) ? Ops<T>::nan_() : (T)0;
+            s2 = (c.bits & MCD_Q_NAN_DIRECTION) ? Ops<T>::nan_() : (T)0;
         }
     }
     const T uphi = Ops<T>::unit(r.w);
@@ -459,7 +459,7 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
         ev->ch = ch;
     }
     const bool left = L.outcome != MCD_OUT_NONE;
-    if (!left || (c.quirks & MCD_Q_CROSSING_STEP)) lane_lose(L, c, W);
+    if (!left || (c.bits & MCD_Q_CROSSING_STEP)) lane_lose(L, c, W);
     if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
     return ch;
 }
@@ -513,7 +513,7 @@ __device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec,
         ev->ch = MCD_CH_RUTH;
     }
     const bool left = L.outcome != MCD_OUT_NONE;
-    if (!left || (c.quirks & MCD_Q_CROSSING_STEP)) lane_lose(L, c, dE);
+    if (!left || (c.bits & MCD_Q_CROSSING_STEP)) lane_lose(L, c, dE);
     if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
     return MCD_CH_RUTH;
 }

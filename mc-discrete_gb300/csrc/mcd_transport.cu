@@ -315,12 +315,12 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
             const SimConst<float>& c = s_c[sim];
             EventOut<float> ev;
             int ch;
-            if (MODE_MIX == 0 || c.mode == MCD_MODE_DS)
+            if (MODE_MIX == 0 || !(c.bits & kBitCont))
                 ch = ds_event<float, REC>(L, c, c.first + local, &ev, !inline_sigma && c.sig != nullptr);
             else
                 ch = cont_event<float, REC>(L, c, c.first + local, &ev);
             if (REC && ch >= 0) ring_append(ring, (uint32_t)local, L.step, ev);
-            if (ch >= 0 && (c.tally_flags & MCD_TALLY_CHANNELS)) atomicAdd(&s_t[sim].channel[ch], 1u);
+            if (ch >= 0 && (c.bits & kBitChan)) atomicAdd(&s_t[sim].channel[ch], 1u);
             if (L.outcome != MCD_OUT_NONE) {
                 st |= finish_electron(c, L, local, s_t[sim], tallies + sim, eo);
                 have = false;

@@ -8,11 +8,14 @@ through the binary-collision model (Watson U^2 two-sample test,
 MC/tools/distributions.py).
 
 Parameters are the reference's test input (tests/testInput.file: Al,
-20 -> 15 keV, normal incidence, Wc 10 eV) with table tolerances of 1e-4 in
-place of its 1e-4 / 1e-7.  The reference accepts U^2 < 0.152 (its 10%
-point) on 200-point samples; here each test draws up to 2000 points and
-requires the asymptotic p-value of U^2 above 1e-3, so that a suite of ten
-such tests does not fail by chance."""
+20 -> 15 keV, normal incidence, Wc 10 eV) with table tolerances tol_E 1e-4
+and tol_W 1e-6 in place of its 1e-4 / 1e-7: the sampled loss is the lower
+W grid point (MC/tools/scattering.py:80-92), which at tol_W 1e-4 lowers the
+median Moller loss by about 1.5% (detectable at 2e4 samples; 0.1% here).
+The reference accepts U^2 < 0.152 (its 10% point) on 200-point samples;
+here each test draws up to 2000 points, from events put in a fixed order,
+and requires the asymptotic p-value of U^2 above 1e-3, so that a suite of
+ten such tests does not fail by chance."""
 import numpy as np
 import pytest
 from scipy import stats
@@ -23,7 +26,7 @@ from _gpu_util import input_par
 
 pytestmark = pytest.mark.gpu
 
-P = input_par("Al", 20000.0, 15000.0, 0.0, Wc=10.0, tol=1e-4)
+P = dict(input_par("Al", 20000.0, 15000.0, 0.0, Wc=10.0, tol=1e-4), tol_W=1e-6)
 N = 20000
 PMIN = 1e-3
 MAT = O.Material("Al")
@@ -36,7 +39,8 @@ def ev():
     assert not g.status & _lib.FLAG_RING_FULL
     e = g.events
     assert e.size == g.tally["events"]
-    return e
+    # the ring's order depends on scheduling: sample from a fixed order
+    return e[np.lexsort((e["step_chan"] >> 5, e["electron"]))]
 
 
 def chan(e):
