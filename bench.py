@@ -42,6 +42,10 @@ N_SHELLS = {"Al": 3, "Si": 3, "Cu": 4, "Au": 8}
 FLOP_PER_EVENT = {k: 176 + 18 * n for k, n in N_SHELLS.items()}   # Si 230, Au 320
 MUFU_PER_EVENT = {k: 17 + 4 * n for k, n in N_SHELLS.items()}     # Si 29, Au 49
 CPU_SAMPLE_PER_SIM = 600
+# DRAM bytes (read + write) of one batched launch of the 64-simulation step,
+# from an ncu capture of that launch (tables and workspace read about once;
+# the figure does not grow with the electrons)
+BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
 
 
 def workload(scale=1.0):
@@ -642,7 +646,8 @@ def run_mcd(args):
         "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": batch.ws_bytes,
                 "d2h_bytes_per_step": int(batch.tallies.numel())},
         "roofline": {"bound": "fp32-issue", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": ach / fp32_peak, "traffic": None,
+                     "frac": ach / fp32_peak, "traffic": BATCHED_DRAM_BYTES if args.scale == 1.0 else None,
+                     "traffic_note": "DRAM bytes per launch from an ncu capture of the full step",
                      "mufu": {"achieved": ach_mufu, "peak": mufu_peak, "unit": "Tops/s", "frac": ach_mufu / mufu_peak},
                      "peak_note": "nominal %d SMs x 128 FP32 lanes x 2 (MUFU: x16) at sm_max_mhz %.0f" % (sms, fmax / 1e6)},
         "cpu_baseline": {"value": cpu_v, "unit": "events/s", "cores": cpu["threads"], "kind": "port",
