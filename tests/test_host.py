@@ -170,3 +170,23 @@ def test_sim_struct_from_input():
     assert s.num_el == 64 and s.seed == 3 and s.s_tilt == 70.0
     with pytest.raises(NotImplementedError):
         engine.make_sim(dict(p, elastic="Mott"), 1)
+
+
+def test_new_fields_are_validated_before_any_gpu_work():
+    """Elastic model codes, the diffraction switch and the adjoint's quantity
+    are checked on the host: a bad value returns MCD_EINVAL before a launch."""
+    from mcd import engine
+    L = _lib.lib()
+    p = config.parse_input(INPUT)
+    mat = _lib.material("Al")
+    s = engine.make_sim(p, 16)                       # continuous mode, Al
+    s.elastic = 7
+    assert L.mcd_run(C.byref(s), C.byref(mat), None, None, 1, None, None, 1, 128, None) == _lib.EINVAL
+    s = engine.make_sim(p, 16)
+    s.diff_mfp = 1                                   # continuous mode has no diffraction channel
+    assert L.mcd_run(C.byref(s), C.byref(mat), None, None, 1, None, None, 1, 128, None) == _lib.EINVAL
+    h = _lib.SoftHist(64, 5, 0.0, 1.0, 0.1)          # unknown quantity
+    buf = _lib.AdjointBuf(1, 1, 1, 4, 0)
+    assert L.mcd_adjoint_forward(C.byref(engine.make_sim(p, 16)), C.byref(mat), C.byref(h), C.byref(buf), 1, None,
+                                 1, None) == _lib.EINVAL
+    assert L.mcd_project_detector(None, 5, _lib.FP32, 20.0, 0.0, 0.0, 0.0, None, None) == _lib.EINVAL
