@@ -675,7 +675,7 @@ def main():
     ap.add_argument("--refill", type=int, default=0, help="batched refill granularity (0: autotune)")
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0, help="batched tune variant bits, with --block")
-    ap.add_argument("--plain-block", type=int, default=128)
+    ap.add_argument("--plain-block", type=int, default=0, help="plain launch block size (0: automatic)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="multiply every num_el (profiling of small cases); 1 = the benchmark workload")

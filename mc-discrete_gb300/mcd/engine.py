@@ -192,7 +192,7 @@ EVENT_DTYPE = np.dtype([("electron", "<u4"), ("step_chan", "<u4"), ("E", "<f4"),
                         ("y", "<f4"), ("z", "<f4")])
 
 
-def launch(sim, mat, tables, bufs, block_size=128, stream=None):
+def launch(sim, mat, tables, bufs, block_size=0, stream=None):
     """Enqueue one mcd_run on `stream` (torch's current stream by default)."""
     torch = _torch()
     st = stream if stream is not None else torch.cuda.current_stream(bufs.device)
@@ -230,7 +230,7 @@ def collect(bufs):
 
 def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", electrons=True, ring_capacity=0,
         tally_channels=False, hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
-        J_scale=1.0, n_scale=1.0, block_size=128, device="cuda", tables=None):
+        J_scale=1.0, n_scale=1.0, block_size=0, device="cuda", tables=None):
     """Run one simulation to completion and return its results on the host."""
     _torch()
     p = with_defaults(input_par)
