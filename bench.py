@@ -434,7 +434,8 @@ def detector_bench(args, dev):
 
 
 STREAM_WORKLOAD = ("DS Au, E0 30 keV, Emin 0.5 keV, tilt 70 deg, Wc 50 eV, tol 1e-4, every event streamed "
-                   "as a 40-byte record through two device rings to pinned host memory")
+                   "with its step length, channel, W, polar angle and position (32-byte records) through two "
+                   "device rings to pinned host memory")
 
 
 def stream_bench(args, dev):
@@ -445,7 +446,9 @@ def stream_bench(args, dev):
     p = dict(material="Au", E0=30000.0, Emin=500.0, s_tilt=70.0, Wc=50.0, tol_E=1e-4, tol_W=1e-4, mode="DS",
              num_el=n)
     chunk = min(n, 1_000_000)
-    es = EventStream(p, chunk=chunk, seed=args.seed, events_per_electron=950.0, device=dev)
+    from mcd import _lib
+    fields = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS
+    es = EventStream(p, chunk=chunk, seed=args.seed, events_per_electron=950.0, device=dev, fields=fields)
     seen = [0]
 
     def consumer(rec, c):            # the host side only counts what arrives
@@ -457,7 +460,8 @@ def stream_bench(args, dev):
     st = es.run(consumer)
     return {"workload": STREAM_WORKLOAD, "num_el": n, "chunk": chunk, "events": st["events"],
             "records_received": seen[0], "wall_s": st["wall_s"], "events_per_s": st["events"] / st["wall_s"],
-            "drain_GB_per_s": st["bytes"] / st["wall_s"] / 1e9, "ring_GB": es.cap * 40 / 1e9,
+            "drain_GB_per_s": st["bytes"] / st["wall_s"] / 1e9, "record_bytes": es.rec_bytes,
+            "ring_GB": es.cap * es.rec_bytes / 1e9,
             "reruns": st["reruns"], "gpu_launches": len(es.batches)}
 
 

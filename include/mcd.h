@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 5
+#define MCD_ABI_VERSION 6
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -192,12 +192,29 @@ typedef struct mcd_event {
     float x, y, z;           /* position at the start of the event, A         */
 } mcd_event;                 /* 40 bytes                                      */
 
+/* Fields of a ring record after its 8-byte header (electron,
+ * event << 5 | channel), in this order, 4 bytes each (position: 12), the
+ * scatter_output columns they carry in brackets (MC/tools/fileTools.py:
+ * 193-242).  A mask of 0 selects all of them: the mcd_event layout.        */
+#define MCD_EV_E     0x01u      /* E before the event ['E']                  */
+#define MCD_EV_W     0x02u      /* energy loss ['E_loss']                    */
+#define MCD_EV_PATHL 0x04u      /* step length ['pathl']                     */
+#define MCD_EV_C2    0x08u      /* cos^2(theta/2) ['pol_angle']              */
+#define MCD_EV_PHI   0x10u      /* halfPhi ['az_angle']                      */
+#define MCD_EV_POS   0x20u      /* x, y, z at the start ['position']         */
+#define MCD_EV_ALL   0x3fu
 typedef struct mcd_event_ring {
-    mcd_event* rec;                  /* device, capacity records              */
+    void* rec;                       /* device, capacity records of
+                                        mcd_event_bytes(fields) bytes each    */
     unsigned long long capacity;
     unsigned long long* cursor;      /* device; records reserved so far; the
                                         ones at index >= capacity are dropped */
+    uint32_t fields;                 /* MCD_EV_* mask, 0 = all                */
+    uint32_t reserved;
 } mcd_event_ring;
+
+/* Bytes of one ring record for a field mask (host).                          */
+size_t mcd_event_bytes(uint32_t fields);
 
 /* ---- launch tuning of the batched kernel -------------------------------- */
 typedef struct mcd_tune {

@@ -532,10 +532,13 @@ __device__ __forceinline__ void ring_append(const mcd_event_ring& ring, uint32_t
     if (lane == leader) base = atomicAdd(ring.cursor, (unsigned long long)__popc(mask));
     base = __shfl_sync(mask, base, leader);
     const unsigned long long slot = base + rank;
-    if (slot < ring.capacity) {
+    if (slot >= ring.capacity) return;
+    const uint32_t head = ((uint32_t)(step - 1) << 5) | (uint32_t)(ev.ch & 31);
+    const uint32_t f = ring.fields & MCD_EV_ALL;
+    if (f == 0 || f == MCD_EV_ALL) {
         mcd_event e;
         e.electron = electron;
-        e.step_chan = ((uint32_t)(step - 1) << 5) | (uint32_t)(ev.ch & 31);
+        e.step_chan = head;
         e.E = (float)ev.E;
         e.W = (float)ev.W;
         e.pathl = (float)ev.pathl;
@@ -544,7 +547,24 @@ __device__ __forceinline__ void ring_append(const mcd_event_ring& ring, uint32_t
         e.x = (float)ev.x;
         e.y = (float)ev.y;
         e.z = (float)ev.z;
-        ring.rec[slot] = e;
+        static_cast<mcd_event*>(ring.rec)[slot] = e;
+        return;
+    }
+    // the selected columns only, packed after the header
+    const int words = 2 + __popc(f & 0x1fu) + ((f & MCD_EV_POS) ? 3 : 0);
+    uint32_t* p = static_cast<uint32_t*>(ring.rec) + slot * (unsigned long long)words;
+    p[0] = electron;
+    p[1] = head;
+    int o = 2;
+    if (f & MCD_EV_E) p[o++] = __float_as_uint((float)ev.E);
+    if (f & MCD_EV_W) p[o++] = __float_as_uint((float)ev.W);
+    if (f & MCD_EV_PATHL) p[o++] = __float_as_uint((float)ev.pathl);
+    if (f & MCD_EV_C2) p[o++] = __float_as_uint((float)ev.c2);
+    if (f & MCD_EV_PHI) p[o++] = __float_as_uint((float)ev.half_phi);
+    if (f & MCD_EV_POS) {
+        p[o++] = __float_as_uint((float)ev.x);
+        p[o++] = __float_as_uint((float)ev.y);
+        p[o] = __float_as_uint((float)ev.z);
     }
 }
 

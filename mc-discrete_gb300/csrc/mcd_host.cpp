@@ -54,6 +54,13 @@ void copy_name(char* dst, size_t cap, const char* src) {
 
 extern "C" int mcd_abi_version(void) { return MCD_ABI_VERSION; }
 
+extern "C" size_t mcd_event_bytes(uint32_t fields) {
+    uint32_t f = fields & MCD_EV_ALL;
+    if (f == 0) f = MCD_EV_ALL;
+    size_t words = 2 + (size_t)__builtin_popcount(f & 0x1fu) + ((f & MCD_EV_POS) ? 3 : 0);
+    return 4 * words;
+}
+
 extern "C" const char* mcd_strerror(int code) {
     switch (code) {
         case MCD_OK: return "ok";

@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 MAX_SHELLS = 8
 GUIDE = 256
 MAX_CHANNELS = 16
@@ -36,6 +36,9 @@ MODE_DS, MODE_CONT = 0, 1
 BETHE = {"classical": 0, "JL": 1, "explicit": 2}
 FP32, FP64 = 0, 1
 ADJ_EXIT_E, ADJ_MAX_DEPTH = 0, 1
+# event-ring record fields (after the electron / event-and-channel header)
+EV_E, EV_W, EV_PATHL, EV_C2, EV_PHI, EV_POS = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
+EV_ALL = 0x3f
 TABLE_MOLLER, TABLE_GRYZ = 0, 1
 
 Q_CROSSING_STEP = 0x1
@@ -160,6 +163,8 @@ class EventRing(C.Structure):
         ("rec", C.c_void_p),
         ("capacity", C.c_uint64),
         ("cursor", C.c_void_p),
+        ("fields", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
 
@@ -218,6 +223,7 @@ SIGNATURES = {
     "mcd_run_batched_noalloc": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
                                           C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                           C.c_void_p, C.POINTER(Tune), C.c_void_p, C.c_void_p]),
+    "mcd_event_bytes": (C.c_size_t, [C.c_uint32]),
     "mcd_project_detector": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_void_p, C.c_void_p]),
     "mcd_run_batched_ring": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(Tune), C.POINTER(EventRing),

@@ -126,7 +126,7 @@ def tally_from_bytes(buf):
 class RunBuffers:
     """Device buffers of one simulation (re-usable across launches)."""
 
-    def __init__(self, num_el, precision=_lib.FP32, electrons=True, ring_capacity=0, device="cuda"):
+    def __init__(self, num_el, precision=_lib.FP32, electrons=True, ring_capacity=0, device="cuda", ring_fields=0):
         torch = _torch()
         self.device = torch.device(device)
         self.num_el = int(num_el)
@@ -148,8 +148,9 @@ class RunBuffers:
                 n_events=torch.zeros(n, dtype=torch.int32, device=self.device),
             )
         self.ring = None
+        self.ring_fields = int(ring_fields)
         if ring_capacity:
-            self.ring = torch.zeros((int(ring_capacity), C.sizeof(_lib.Event)), dtype=torch.uint8,
+            self.ring = torch.zeros((int(ring_capacity), event_bytes(self.ring_fields)), dtype=torch.uint8,
                                     device=self.device)
             self.cursor = torch.zeros(1, dtype=torch.int64, device=self.device)
 
@@ -170,7 +171,7 @@ class RunBuffers:
     def ring_struct(self):
         if self.ring is None:
             return None
-        return _lib.EventRing(self.ring.data_ptr(), self.ring.shape[0], self.cursor.data_ptr())
+        return _lib.EventRing(self.ring.data_ptr(), self.ring.shape[0], self.cursor.data_ptr(), self.ring_fields, 0)
 
 
 class RunResult:
@@ -190,6 +191,24 @@ class RunResult:
 EVENT_DTYPE = np.dtype([("electron", "<u4"), ("step_chan", "<u4"), ("E", "<f4"), ("W", "<f4"),
                         ("pathl", "<f4"), ("c2", "<f4"), ("half_phi", "<f4"), ("x", "<f4"),
                         ("y", "<f4"), ("z", "<f4")])
+_EV_NAMES = ((_lib.EV_E, ("E",)), (_lib.EV_W, ("W",)), (_lib.EV_PATHL, ("pathl",)), (_lib.EV_C2, ("c2",)),
+             (_lib.EV_PHI, ("half_phi",)), (_lib.EV_POS, ("x", "y", "z")))
+
+
+def event_dtype(fields=0):
+    """Record dtype of a ring written with an MCD_EV_* field mask (0 = all)."""
+    f = int(fields) & _lib.EV_ALL
+    if f in (0, _lib.EV_ALL):
+        return EVENT_DTYPE
+    names = [("electron", "<u4"), ("step_chan", "<u4")]
+    for bit, cols in _EV_NAMES:
+        if f & bit:
+            names += [(c, "<f4") for c in cols]
+    return np.dtype(names)
+
+
+def event_bytes(fields=0):
+    return event_dtype(fields).itemsize
 
 
 def launch(sim, mat, tables, bufs, block_size=0, stream=None):
@@ -222,7 +241,7 @@ def collect(bufs):
     if bufs.ring is not None:
         total = int(bufs.cursor.item())
         k = min(total, bufs.ring.shape[0])
-        events = bufs.ring[:k].cpu().numpy().view(EVENT_DTYPE).reshape(-1)
+        events = bufs.ring[:k].cpu().numpy().view(event_dtype(bufs.ring_fields)).reshape(-1)
         if total > bufs.ring.shape[0]:
             status |= _lib.FLAG_RING_FULL
     return RunResult(tally, status, electrons, events, total)

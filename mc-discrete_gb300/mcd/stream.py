@@ -5,7 +5,9 @@ back to the parent process and appends them to an HDF5 store
 (MC/tools/fileTools.py:193-242, MC/doScatter.py:99-119).  Here the electrons
 of a simulation are cut into chunks; each chunk runs as one batched
 persistent launch whose every event is appended to a device ring
-(mcd_run_batched_ring).  Two rings alternate: while chunk c+1 is being
+(mcd_run_batched_ring), as a full 40-byte record or with only the fields a
+field mask selects (the scatter_output columns wanted; 8-byte header plus
+4 bytes per column).  Two rings alternate: while chunk c+1 is being
 transported, chunk c's records are copied to pinned host memory on a second
 stream, in pieces handed to a consumer callback.  A chunk whose events do
 not fit its ring is re-run with a larger ring; the counter-based random
@@ -18,9 +20,7 @@ import numpy as np
 
 from . import _lib
 from .config import with_defaults
-from .engine import EVENT_DTYPE, Batch, _torch
-
-REC_BYTES = C.sizeof(_lib.Event)
+from .engine import Batch, _torch, event_dtype
 
 
 class EventStream:
@@ -35,12 +35,15 @@ class EventStream:
     """
 
     def __init__(self, input_par, chunk=1_000_000, seed=0, ring_events=None, piece_bytes=1 << 30,
-                 events_per_electron=None, tune=None, device="cuda"):
+                 events_per_electron=None, tune=None, device="cuda", fields=0):
         torch = _torch()
         self.p = with_defaults(input_par)
         self.num_el = int(self.p["num_el"])
         self.chunk = int(min(chunk, self.num_el))
         self.seed = int(seed)
+        self.fields = int(fields)
+        self.dtype = event_dtype(self.fields)
+        self.rec_bytes = self.dtype.itemsize
         self.device = torch.device(device)
         self.tune = tune if tune is not None else _lib.Tune(256, 0, 1, 0, 0)
         self.nchunks = (self.num_el + self.chunk - 1) // self.chunk
@@ -53,7 +56,7 @@ class EventStream:
                                       first_electron=first))
         epe = events_per_electron or 1000.0
         cap = int(ring_events) if ring_events else int(1.3 * epe * self.chunk) + 4096
-        self.piece = max(REC_BYTES, (int(piece_bytes) // REC_BYTES) * REC_BYTES)
+        self.piece = max(self.rec_bytes, (int(piece_bytes) // self.rec_bytes) * self.rec_bytes)
         self._alloc_rings(cap)
         self.host = [torch.empty(self.piece, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
         self.copy_stream = torch.cuda.Stream(self.device)
@@ -62,7 +65,7 @@ class EventStream:
     def _alloc_rings(self, cap):
         torch = _torch()
         self.cap = int(cap)
-        self.rings = [torch.empty(self.cap * REC_BYTES, dtype=torch.uint8, device=self.device) for _ in range(2)]
+        self.rings = [torch.empty(self.cap * self.rec_bytes, dtype=torch.uint8, device=self.device) for _ in range(2)]
         self.cursors = [torch.zeros(1, dtype=torch.int64, device=self.device) for _ in range(2)]
 
     def _launch(self, c, slot, stream):
@@ -70,7 +73,7 @@ class EventStream:
         b.tallies.zero_()
         b.status.zero_()
         self.cursors[slot].zero_()
-        ring = _lib.EventRing(self.rings[slot].data_ptr(), self.cap, self.cursors[slot].data_ptr())
+        ring = _lib.EventRing(self.rings[slot].data_ptr(), self.cap, self.cursors[slot].data_ptr(), self.fields, 0)
         code = _lib.lib().mcd_run_batched_ring(b.ws_ptr, b.n, b.tallies.data_ptr(), C.byref(self.tune),
                                                C.byref(ring), b.status.data_ptr(), stream.cuda_stream)
         _lib.check("mcd_run_batched_ring", code)
@@ -115,7 +118,7 @@ class EventStream:
                     self._launch(o, o % 2, cs)
                     done[o % 2].record(cs)
                 continue
-            nbytes = n * REC_BYTES
+            nbytes = n * self.rec_bytes
             off = 0
             ring = self.rings[slot]
             while off < nbytes:
@@ -125,7 +128,7 @@ class EventStream:
                     hb[:k].copy_(ring[off:off + k], non_blocking=True)
                 self.copy_stream.synchronize()
                 if consumer is not None:
-                    consumer(hb[:k].numpy().view(EVENT_DTYPE), c)
+                    consumer(hb[:k].numpy().view(self.dtype), c)
                 off += k
             with torch.cuda.stream(self.copy_stream):
                 freed[slot].record(self.copy_stream)

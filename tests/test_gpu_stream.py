@@ -74,3 +74,18 @@ def test_stream_with_tables_delivers_every_tallied_event(single):
     first = np.r_[True, rec["electron"][1:] != rec["electron"][:-1]]
     assert np.all(steps[first] == 0)
     assert np.all(np.diff(steps)[~first[1:]] == 1)
+
+
+def test_stream_of_selected_columns_equals_full_records(single):
+    """Records carrying only step length, W, cos^2(theta/2) and position (the
+    scatter_output columns of the streamed Au configuration) hold the same
+    values as the full records."""
+    ref, _ = single
+    fields = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS
+    es = EventStream(P, chunk=4000, seed=21, events_per_electron=450.0, tune=INLINE, fields=fields)
+    rec, stats = collect_stream(es)
+    assert rec.dtype.itemsize == 32 and stats["bytes"] == rec.size * 32
+    assert rec.size == ref.size
+    rec = key(rec)
+    for f in ("electron", "step_chan", "W", "pathl", "c2", "x", "y", "z"):
+        assert np.array_equal(rec[f], ref[f]), f

@@ -39,7 +39,7 @@ def test_struct_layouts_match():
 
 def test_abi_and_errors():
     L = _lib.lib()
-    assert L.mcd_abi_version() == _lib.ABI_VERSION == 5
+    assert L.mcd_abi_version() == _lib.ABI_VERSION == 6
     assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
     m = _lib.Material()
     assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
@@ -190,3 +190,14 @@ def test_new_fields_are_validated_before_any_gpu_work():
     assert L.mcd_adjoint_forward(C.byref(engine.make_sim(p, 16)), C.byref(mat), C.byref(h), C.byref(buf), 1, None,
                                  1, None) == _lib.EINVAL
     assert L.mcd_project_detector(None, 5, _lib.FP32, 20.0, 0.0, 0.0, 0.0, None, None) == _lib.EINVAL
+
+
+def test_event_record_sizes_agree_with_library():
+    from mcd import engine
+    L = _lib.lib()
+    assert L.mcd_event_bytes(0) == 40 == L.mcd_event_bytes(_lib.EV_ALL) == C.sizeof(_lib.Event)
+    for mask in range(64):
+        assert engine.event_dtype(mask).itemsize == L.mcd_event_bytes(mask), mask
+    cfg = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS
+    assert L.mcd_event_bytes(cfg) == 32
+    assert engine.event_dtype(cfg).names == ("electron", "step_chan", "W", "pathl", "c2", "x", "y", "z")
