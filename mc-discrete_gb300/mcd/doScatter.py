@@ -53,6 +53,19 @@ def type_labels(mat, mode, elastic):
     return np.array(names)
 
 
+# scatter_output column -> ring record fields it needs ('type' is in the header)
+COL_FIELDS = {"type": 0, "E": _lib.EV_E, "E_loss": _lib.EV_W, "pol_angle": _lib.EV_C2, "az_angle": _lib.EV_PHI,
+              "pathl": _lib.EV_PATHL, "position": _lib.EV_POS, "energy": _lib.EV_E | _lib.EV_W}
+
+
+def ring_fields(sc_cols):
+    """The ring field mask that carries exactly the requested columns."""
+    f = 0
+    for c in sc_cols:
+        f |= COL_FIELDS[c]
+    return f if f else _lib.EV_PATHL     # 'type' alone: the smallest record with a field
+
+
 def chunk_tables(res, n, el_cols, sc_cols, labels):
     """Column arrays of one chunk of n electrons from its device rows."""
     e = res.electrons
@@ -183,7 +196,7 @@ def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_e
         sim = make_sim(p, n, seed, first)
         cap = int(1.3 * epe * n) + 4096 if sc_cols else 0
         while True:
-            bufs = RunBuffers(n, _lib.FP32, True, cap)
+            bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=ring_fields(sc_cols))
             bufs.zero()
             launch(sim, mat, tables, bufs)
             res = collect(bufs)

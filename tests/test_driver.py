@@ -47,3 +47,11 @@ def test_chunk_tables():
     assert set(scats) == {"type", "E", "E_loss", "x", "y", "z", "energy"}
     cont = doScatter.type_labels(mat, _lib.MODE_CONT, "Ruth_nigram")
     assert cont[_lib.CH_RUTH] == "Ruth_nigram"
+
+
+def test_ring_fields_follow_requested_columns():
+    assert doScatter.ring_fields(["type", "E_loss", "pol_angle", "pathl", "position"]) == (
+        _lib.EV_W | _lib.EV_C2 | _lib.EV_PATHL | _lib.EV_POS)
+    assert doScatter.ring_fields(["energy"]) == _lib.EV_E | _lib.EV_W
+    assert doScatter.ring_fields(list(doScatter.SCAT_COLS)) == _lib.EV_ALL
+
