@@ -62,7 +62,7 @@ def ring_fields(sc_cols):
     """The ring field mask that carries exactly the requested columns."""
     f = 0
     for c in sc_cols:
-        f |= COL_FIELDS[c]
+        f |= COL_FIELDS.get(c, 0)
     return f if f else _lib.EV_PATHL     # 'type' alone: the smallest record with a field
 
 

@@ -121,8 +121,11 @@ def _run_traj(inputPar, numTraj, thingsToSave):
               if mode == _lib.MODE_DS else None)
     want_events = bool(thingsToSave.get("scat_output"))
     cap = n * 2048 if want_events else 0
+    # the ring records carry only the requested scatter_output columns
+    from .doScatter import ring_fields
+    fields = ring_fields(list(thingsToSave.get("scat_output", [])))
     while True:
-        bufs = RunBuffers(n, _lib.FP32, True, cap)
+        bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=fields)
         bufs.zero()
         launch(sim, mat, tables, bufs)
         res = collect(bufs)
