@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 6
+#define MCD_ABI_VERSION 7
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -132,7 +132,9 @@ typedef struct mcd_sim {
     double s_tilt;           /* degrees                                       */
     double Wc;               /* Moller cut-off, eV (DS)                       */
     double thickness;        /* A; >= 1e30 means semi-infinite                */
-    int64_t max_scatt;
+    int64_t max_scatt;       /* events before 'long' (MC/tools/singleScatter.py:
+                                19-23); <= 0 or above 2^32 - 1 means 2^32 - 1,
+                                the range of the Philox event counter word   */
     int64_t num_el;
     uint64_t first_electron; /* Philox electron index of electron 0           */
     uint64_t seed;           /* Philox key                                    */
@@ -226,8 +228,7 @@ typedef struct mcd_tune {
                                 instead of the 64-register one; bit 1: evaluate
                                 cross sections inline instead of from the
                                 tables mcd_batch_prepare builds              */
-    int64_t step_budget;     /* 0 = run to completion; else events per lane
-                                before the kernel parks its electrons         */
+    int64_t reserved;        /* must be 0                                     */
 } mcd_tune;
 
 /* ====================== host-only entry points ========================== */

@@ -88,7 +88,7 @@ struct SimConst {
     uint32_t tally_flags;
     uint32_t sim_id;
     uint32_t key0, key1;
-    int64_t max_scatt;
+    uint32_t max_scatt;   // events before 'long', at most 2^32 - 1 (the counter word)
     uint64_t first;
     int64_t num_el;
     int32_t hE, hT;
@@ -198,7 +198,7 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     c.sim_id = s.sim_id;
     c.key0 = (uint32_t)(s.seed & 0xffffffffull);
     c.key1 = (uint32_t)(s.seed >> 32);
-    c.max_scatt = s.max_scatt > 0 ? s.max_scatt : INT64_MAX;
+    c.max_scatt = (s.max_scatt > 0 && s.max_scatt < (int64_t)UINT32_MAX) ? (uint32_t)s.max_scatt : UINT32_MAX;
     c.first = s.first_electron;
     c.num_el = s.num_el;
     c.hE = s.hist_E_bins;

@@ -205,7 +205,7 @@ struct Lane {
     T E, x, y, z, dx, dy, dz, yx, yy, yz;
     T E_row;   // energy of the first outcome row
     T max_z;
-    int64_t step;
+    uint32_t step;   // events so far (Philox counter word 0)
     uint32_t outcome;
     uint32_t flags;
     uint32_t nan_n, clamp_n, lpath_n;
@@ -357,19 +357,27 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     return MCD_CH_GRYZ0 + (j - 2);
 }
 
-template <class T, bool REC, class C>
-__device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev,
-                                        bool use_tab = false) {
-    const T E = L.E;
-    // --- 'long' check first (MC/tools/singleScatter.py:19-23)
+// The 'long' check that opens every event (MC/tools/singleScatter.py:19-23).
+template <class T, class C>
+__device__ __forceinline__ bool lane_long(Lane<T>& L, const C& c) {
     if (L.step >= c.max_scatt) {
         L.outcome = MCD_OUT_LONG;
-        L.E_row = E;
-        return -1;
+        L.E_row = L.E;
+        return true;
     }
-    const uint4 r = philox(make_uint4((uint32_t)L.step, (uint32_t)elec, (uint32_t)(elec >> 32), c.sim_id),
-                           c.key0, c.key1);
-    L.step += 1;
+    return false;
+}
+
+__device__ __forceinline__ uint4 event_counter(uint32_t step, uint64_t elec, uint32_t sim_id) {
+    return make_uint4(step, (uint32_t)elec, (uint32_t)(elec >> 32), sim_id);
+}
+
+// One DS event from its four random words r (the step counter already
+// advanced).  Returns the channel code.
+template <class T, bool REC, class C>
+__device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r, EventOut<T>* ev,
+                                          bool use_tab = false) {
+    const T E = L.E;
     int ch = MCD_CH_QUINN;
     T inv_tot;
     if (use_tab) {
@@ -464,21 +472,22 @@ __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, E
     return ch;
 }
 
+template <class T, bool REC, class C>
+__device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev,
+                                        bool use_tab = false) {
+    if (lane_long(L, c)) return -1;
+    const uint4 r = philox(event_counter(L.step, elec, c.sim_id), c.key0, c.key1);
+    L.step += 1;
+    return ds_event_r<T, REC>(L, c, r, ev, use_tab);
+}
+
 // ---------------------------------------------------------------------------
 // continuous event (MC/tools/scattering.py:753-883 in the order of
 // MC/tools/singleScatter.py:210-239, with the Bethe law the mode names)
 // ---------------------------------------------------------------------------
 template <class T, bool REC, class C>
-__device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev) {
+__device__ __forceinline__ int cont_event_r(Lane<T>& L, const C& c, const uint4 r, EventOut<T>* ev) {
     const T E = L.E;
-    if (L.step >= c.max_scatt) {
-        L.outcome = MCD_OUT_LONG;
-        L.E_row = E;
-        return -1;
-    }
-    const uint4 r = philox(make_uint4((uint32_t)L.step, (uint32_t)elec, (uint32_t)(elec >> 32), c.sim_id),
-                           c.key0, c.key1);
-    L.step += 1;
     const T sR = sig_ruth<T>(c, E);
     const T s = -Ops<T>::ln_step(Ops<T>::unit(r.y)) * Ops<T>::div((T)1, sR);
     if (!(s < (T)1e4)) {
@@ -516,6 +525,14 @@ __device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec,
     if (!left || (c.bits & MCD_Q_CROSSING_STEP)) lane_lose(L, c, dE);
     if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
     return MCD_CH_RUTH;
+}
+
+template <class T, bool REC, class C>
+__device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev) {
+    if (lane_long(L, c)) return -1;
+    const uint4 r = philox(event_counter(L.step, elec, c.sim_id), c.key0, c.key1);
+    L.step += 1;
+    return cont_event_r<T, REC>(L, c, r, ev);
 }
 
 // ---------------------------------------------------------------------------

@@ -557,7 +557,8 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
         if (tune->blocks_per_sm > 0) per_sm = tune->blocks_per_sm;
         if (tune->refill > 0) refill = tune->refill;
     }
-    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32 || (tune && tune->reserved != 0))
+        return MCD_EINVAL;
     const bool lowreg = tune && (tune->variant & 1);
     const int inline_sigma = (tune && (tune->variant & 2)) ? 1 : 0;
     if (lowreg && block > 256) return MCD_EINVAL;
@@ -596,7 +597,8 @@ extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* t
         if (tune->blocks_per_sm > 0) per_sm = tune->blocks_per_sm;
         if (tune->refill > 0) refill = tune->refill;
     }
-    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32 || (tune && tune->reserved != 0))
+        return MCD_EINVAL;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
@@ -678,7 +680,8 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
         if (tune->blocks_per_sm > 0) per_sm = tune->blocks_per_sm;
         if (tune->refill > 0) refill = tune->refill;
     }
-    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32) return MCD_EINVAL;
+    if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32 || (tune && tune->reserved != 0))
+        return MCD_EINVAL;
 
     // pack on the host stack: header (queue = 0), prefix sums, constants
     alignas(256) uint8_t host[kStaticScratchBytes];

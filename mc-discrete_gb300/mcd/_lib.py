@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 6
+ABI_VERSION = 7
 MAX_SHELLS = 8
 GUIDE = 256
 MAX_CHANNELS = 16
@@ -174,7 +174,7 @@ class Tune(C.Structure):
         ("blocks_per_sm", C.c_int32),
         ("refill", C.c_int32),
         ("variant", C.c_int32),
-        ("step_budget", C.c_int64),
+        ("reserved", C.c_int64),
     ]
 
 
