@@ -46,6 +46,11 @@ CPU_SAMPLE_PER_SIM = 600
 # from an ncu capture of that launch (tables and workspace read about once;
 # the figure does not grow with the electrons)
 BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
+# warp instructions issued per event by the batched kernel on this workload,
+# from an ncu capture of a quarter-size launch (2.054e10 instructions for
+# 1.3855e9 events); the issue peak is one warp instruction per scheduler
+# per cycle, 4 schedulers per SM
+WARP_INST_PER_EVENT = 14.82
 
 
 def workload(scale=1.0):
@@ -653,6 +658,10 @@ def run_mcd(args):
                      "frac": ach / fp32_peak, "traffic": BATCHED_DRAM_BYTES if args.scale == 1.0 else None,
                      "traffic_note": "DRAM bytes per launch from an ncu capture of the full step",
                      "mufu": {"achieved": ach_mufu, "peak": mufu_peak, "unit": "Tops/s", "frac": ach_mufu / mufu_peak},
+                     "issue": {"achieved": value * WARP_INST_PER_EVENT / 1e9 / ws,
+                               "peak": sms * 4 * fmax / 1e9, "unit": "G warp instructions/s",
+                               "frac": value * WARP_INST_PER_EVENT / ws / (sms * 4 * fmax),
+                               "inst_per_event_note": "warp instructions per event from an ncu capture"},
                      "peak_note": "nominal %d SMs x 128 FP32 lanes x 2 (MUFU: x16) at sm_max_mhz %.0f" % (sms, fmax / 1e6)},
         "cpu_baseline": {"value": cpu_v, "unit": "events/s", "cores": cpu["threads"], "kind": "port",
                          "sample": "C oracle, min(num_el, %d) electrons of each sim (%d events)"
