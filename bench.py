@@ -439,8 +439,8 @@ def detector_bench(args, dev):
 
 
 STREAM_WORKLOAD = ("DS Au, E0 30 keV, Emin 0.5 keV, tilt 70 deg, Wc 50 eV, tol 1e-4, every event streamed "
-                   "with its step length, channel, W, polar angle and position (32-byte records) through two "
-                   "device rings to pinned host memory")
+                   "with its electron, channel, step length, W, polar angle and position (28-byte records, "
+                   "one-word header) through two device rings to pinned host memory")
 
 
 def stream_bench(args, dev):
@@ -452,7 +452,7 @@ def stream_bench(args, dev):
              num_el=n)
     chunk = min(n, 1_000_000)
     from mcd import _lib
-    fields = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS
+    fields = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS | _lib.EV_PACKED_HEAD
     es = EventStream(p, chunk=chunk, seed=args.seed, events_per_electron=950.0, device=dev, fields=fields)
     seen = [0]
 

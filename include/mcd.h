@@ -44,7 +44,8 @@ enum {
 #define MCD_FLAG_CLAMPED     0x08u /* continuous: energy loss >= E, clamped to E   */
 #define MCD_FLAG_LONG_PATH   0x10u /* continuous: a step of 1e4 A or more          */
 #define MCD_FLAG_LONG        0x20u /* an electron reached max_scatt                */
-#define MCD_FLAG_PARKED      0x40u /* batched: electrons left in flight (budget)   */
+#define MCD_FLAG_RING_INDEX  0x40u /* packed ring header: an electron index of
+                                      2^28 or more; its records were dropped   */
 #define MCD_FLAG_CKPT        0x80u /* adjoint: an exiting electron had more events
                                       than checkpoint slots (no gradient)        */
 
@@ -197,21 +198,28 @@ typedef struct mcd_event {
 /* Fields of a ring record after its 8-byte header (electron,
  * event << 5 | channel), in this order, 4 bytes each (position: 12), the
  * scatter_output columns they carry in brackets (MC/tools/fileTools.py:
- * 193-242).  A mask of 0 selects all of them: the mcd_event layout.        */
+ * 193-242).  A column mask of 0 selects all of them: the mcd_event layout.
+ * MCD_EV_PACKED_HEAD replaces the header by one word, electron << 4 |
+ * channel (electron < 2^28), without the event index: the records of one
+ * electron keep their order in the ring (one thread appends them, each
+ * after the last one's slot was returned), so an electron's n-th record
+ * is its event n.                                                          */
 #define MCD_EV_E     0x01u      /* E before the event ['E']                  */
 #define MCD_EV_W     0x02u      /* energy loss ['E_loss']                    */
 #define MCD_EV_PATHL 0x04u      /* step length ['pathl']                     */
 #define MCD_EV_C2    0x08u      /* cos^2(theta/2) ['pol_angle']              */
 #define MCD_EV_PHI   0x10u      /* halfPhi ['az_angle']                      */
 #define MCD_EV_POS   0x20u      /* x, y, z at the start ['position']         */
-#define MCD_EV_ALL   0x3fu
+#define MCD_EV_ALL   0x3fu      /* the column bits                           */
+#define MCD_EV_PACKED_HEAD 0x40u
 typedef struct mcd_event_ring {
     void* rec;                       /* device, capacity records of
                                         mcd_event_bytes(fields) bytes each    */
     unsigned long long capacity;
     unsigned long long* cursor;      /* device; records reserved so far; the
                                         ones at index >= capacity are dropped */
-    uint32_t fields;                 /* MCD_EV_* mask, 0 = all                */
+    uint32_t fields;                 /* MCD_EV_* columns (0 = all), with
+                                        MCD_EV_PACKED_HEAD or not            */
     uint32_t reserved;
 } mcd_event_ring;
 

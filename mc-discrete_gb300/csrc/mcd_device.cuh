@@ -539,8 +539,10 @@ __device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec,
 // warp-aggregated append of one record per calling lane to the event ring
 // ---------------------------------------------------------------------------
 template <class T>
-__device__ __forceinline__ void ring_append(const mcd_event_ring& ring, uint32_t electron, int64_t step,
-                                            const EventOut<T>& ev) {
+__device__ __forceinline__ uint32_t ring_append(const mcd_event_ring& ring, uint32_t electron, uint32_t step,
+                                                const EventOut<T>& ev) {
+    const bool packed = (ring.fields & MCD_EV_PACKED_HEAD) != 0;
+    if (packed && electron >= (1u << 28)) return MCD_FLAG_RING_INDEX;   // reserves no slot
     const unsigned mask = __activemask();
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(mask) - 1;
@@ -549,13 +551,12 @@ __device__ __forceinline__ void ring_append(const mcd_event_ring& ring, uint32_t
     if (lane == leader) base = atomicAdd(ring.cursor, (unsigned long long)__popc(mask));
     base = __shfl_sync(mask, base, leader);
     const unsigned long long slot = base + rank;
-    if (slot >= ring.capacity) return;
-    const uint32_t head = ((uint32_t)(step - 1) << 5) | (uint32_t)(ev.ch & 31);
+    if (slot >= ring.capacity) return 0;
     const uint32_t f = ring.fields & MCD_EV_ALL;
-    if (f == 0 || f == MCD_EV_ALL) {
+    if (!packed && (f == 0 || f == MCD_EV_ALL)) {
         mcd_event e;
         e.electron = electron;
-        e.step_chan = head;
+        e.step_chan = ((step - 1) << 5) | (uint32_t)(ev.ch & 31);
         e.E = (float)ev.E;
         e.W = (float)ev.W;
         e.pathl = (float)ev.pathl;
@@ -565,24 +566,32 @@ __device__ __forceinline__ void ring_append(const mcd_event_ring& ring, uint32_t
         e.y = (float)ev.y;
         e.z = (float)ev.z;
         static_cast<mcd_event*>(ring.rec)[slot] = e;
-        return;
+        return 0;
     }
     // the selected columns only, packed after the header
-    const int words = 2 + __popc(f & 0x1fu) + ((f & MCD_EV_POS) ? 3 : 0);
+    const uint32_t cols = f ? f : MCD_EV_ALL;
+    const int words = (packed ? 1 : 2) + __popc(cols & 0x1fu) + ((cols & MCD_EV_POS) ? 3 : 0);
     uint32_t* p = static_cast<uint32_t*>(ring.rec) + slot * (unsigned long long)words;
-    p[0] = electron;
-    p[1] = head;
-    int o = 2;
-    if (f & MCD_EV_E) p[o++] = __float_as_uint((float)ev.E);
-    if (f & MCD_EV_W) p[o++] = __float_as_uint((float)ev.W);
-    if (f & MCD_EV_PATHL) p[o++] = __float_as_uint((float)ev.pathl);
-    if (f & MCD_EV_C2) p[o++] = __float_as_uint((float)ev.c2);
-    if (f & MCD_EV_PHI) p[o++] = __float_as_uint((float)ev.half_phi);
-    if (f & MCD_EV_POS) {
+    int o;
+    if (packed) {
+        p[0] = (electron << 4) | (uint32_t)(ev.ch & 15);
+        o = 1;
+    } else {
+        p[0] = electron;
+        p[1] = ((step - 1) << 5) | (uint32_t)(ev.ch & 31);
+        o = 2;
+    }
+    if (cols & MCD_EV_E) p[o++] = __float_as_uint((float)ev.E);
+    if (cols & MCD_EV_W) p[o++] = __float_as_uint((float)ev.W);
+    if (cols & MCD_EV_PATHL) p[o++] = __float_as_uint((float)ev.pathl);
+    if (cols & MCD_EV_C2) p[o++] = __float_as_uint((float)ev.c2);
+    if (cols & MCD_EV_PHI) p[o++] = __float_as_uint((float)ev.half_phi);
+    if (cols & MCD_EV_POS) {
         p[o++] = __float_as_uint((float)ev.x);
         p[o++] = __float_as_uint((float)ev.y);
         p[o] = __float_as_uint((float)ev.z);
     }
+    return 0;
 }
 
 }  // namespace mcd

@@ -57,7 +57,8 @@ extern "C" int mcd_abi_version(void) { return MCD_ABI_VERSION; }
 extern "C" size_t mcd_event_bytes(uint32_t fields) {
     uint32_t f = fields & MCD_EV_ALL;
     if (f == 0) f = MCD_EV_ALL;
-    size_t words = 2 + (size_t)__builtin_popcount(f & 0x1fu) + ((f & MCD_EV_POS) ? 3 : 0);
+    const size_t head = (fields & MCD_EV_PACKED_HEAD) ? 1 : 2;
+    size_t words = head + (size_t)__builtin_popcount(f & 0x1fu) + ((f & MCD_EV_POS) ? 3 : 0);
     return 4 * words;
 }
 

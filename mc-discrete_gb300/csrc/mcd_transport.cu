@@ -148,11 +148,11 @@ __global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* 
             const int ch = (MODE == MCD_MODE_DS) ? ds_event<T, REC>(L, c, elec, &ev)
                                                  : cont_event<T, REC>(L, c, elec, &ev);
             if (ch >= 0) {
-                if (REC) ring_append(ring, (uint32_t)i, L.step, ev);
+                if (REC) st |= ring_append(ring, (uint32_t)i, L.step, ev);
                 if (chan) atomicAdd(&bt.channel[ch], 1u);
             }
         }
-        st = finish_electron(c, L, i, bt, tally, eo);
+        st |= finish_electron(c, L, i, bt, tally, eo);
     }
     or_status(status, st);
     __syncthreads();
@@ -319,7 +319,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
                 ch = ds_event<float, REC>(L, c, c.first + local, &ev, !inline_sigma && c.sig != nullptr);
             else
                 ch = cont_event<float, REC>(L, c, c.first + local, &ev);
-            if (REC && ch >= 0) ring_append(ring, (uint32_t)local, L.step, ev);
+            if (REC && ch >= 0) st |= ring_append(ring, (uint32_t)local, L.step, ev);
             if (ch >= 0 && (c.bits & kBitChan)) atomicAdd(&s_t[sim].channel[ch], 1u);
             if (L.outcome != MCD_OUT_NONE) {
                 st |= finish_electron(c, L, local, s_t[sim], tallies + sim, eo);
@@ -471,6 +471,8 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
     mcd_event_ring rg{nullptr, 0, nullptr};
     bool rec = false;
     if (ring && ring->rec && ring->cursor && ring->capacity > 0) {
+        if (ring->fields & ~(MCD_EV_ALL | MCD_EV_PACKED_HEAD)) return MCD_EINVAL;
+        if ((ring->fields & MCD_EV_PACKED_HEAD) && sim->num_el > (1ll << 28)) return MCD_EINVAL;
         rg = *ring;
         rec = true;
     }
@@ -589,6 +591,7 @@ extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* t
                                     const mcd_event_ring* ring, uint32_t* status, void* stream) {
     if (!workspace || !tallies || !status || !ring || !ring->rec || !ring->cursor || ring->capacity == 0)
         return MCD_EINVAL;
+    if (ring->fields & ~(MCD_EV_ALL | MCD_EV_PACKED_HEAD)) return MCD_EINVAL;
     if (nsims <= 0) return MCD_EINVAL;
     if (nsims > kBatchMaxSims) return MCD_ETOOBIG;
     int block = 256, per_sm = 0, refill = 1;

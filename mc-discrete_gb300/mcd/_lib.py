@@ -24,7 +24,7 @@ FLAG_NAN = 0x04
 FLAG_CLAMPED = 0x08
 FLAG_LONG_PATH = 0x10
 FLAG_LONG = 0x20
-FLAG_PARKED = 0x40
+FLAG_RING_INDEX = 0x40
 
 OUT_NONE, OUT_BKS, OUT_ABS, OUT_TRSM, OUT_TRDF, OUT_LONG = range(6)
 OUTCOME_NAMES = ("none", "bks", "abs", "trsm", "trdf", "long")
@@ -39,6 +39,7 @@ ADJ_EXIT_E, ADJ_MAX_DEPTH = 0, 1
 # event-ring record fields (after the electron / event-and-channel header)
 EV_E, EV_W, EV_PATHL, EV_C2, EV_PHI, EV_POS = 0x01, 0x02, 0x04, 0x08, 0x10, 0x20
 EV_ALL = 0x3f
+EV_PACKED_HEAD = 0x40   # one-word record header: electron << 4 | channel
 TABLE_MOLLER, TABLE_GRYZ = 0, 1
 
 Q_CROSSING_STEP = 0x1

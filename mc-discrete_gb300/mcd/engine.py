@@ -7,7 +7,6 @@ device buffers (torch tensors) and calls the C ABI on the current stream.
 Everything is device-resident; results are copied back only when asked.
 """
 import ctypes as C
-import math
 
 import numpy as np
 
@@ -196,11 +195,14 @@ _EV_NAMES = ((_lib.EV_E, ("E",)), (_lib.EV_W, ("W",)), (_lib.EV_PATHL, ("pathl",
 
 
 def event_dtype(fields=0):
-    """Record dtype of a ring written with an MCD_EV_* field mask (0 = all)."""
+    """Record dtype of a ring written with an MCD_EV_* field mask (columns,
+    0 = all; with EV_PACKED_HEAD the header is one word 'head')."""
     f = int(fields) & _lib.EV_ALL
-    if f in (0, _lib.EV_ALL):
+    packed = bool(int(fields) & _lib.EV_PACKED_HEAD)
+    if f in (0, _lib.EV_ALL) and not packed:
         return EVENT_DTYPE
-    names = [("electron", "<u4"), ("step_chan", "<u4")]
+    f = f or _lib.EV_ALL
+    names = [("head", "<u4")] if packed else [("electron", "<u4"), ("step_chan", "<u4")]
     for bit, cols in _EV_NAMES:
         if f & bit:
             names += [(c, "<f4") for c in cols]
@@ -209,6 +211,33 @@ def event_dtype(fields=0):
 
 def event_bytes(fields=0):
     return event_dtype(fields).itemsize
+
+
+def unpack_events(rec, fields):
+    """Records of a packed-header ring (in ring order) as records with the
+    'electron' and 'step_chan' header, sorted by electron and event.  An
+    electron's records keep their order in the ring, so its n-th record is
+    its event n; a ring that overflowed has lost records and cannot be
+    unpacked."""
+    fields = int(fields)
+    if not fields & _lib.EV_PACKED_HEAD:
+        return rec
+    out_dt = event_dtype(fields & ~_lib.EV_PACKED_HEAD)
+    head = rec["head"]
+    e = head >> 4
+    order = np.argsort(e, kind="stable")
+    es = e[order]
+    n = es.size
+    first = np.ones(n, dtype=bool)
+    first[1:] = es[1:] != es[:-1]
+    starts = np.flatnonzero(first)
+    step = np.arange(n, dtype=np.int64) - np.repeat(starts, np.diff(np.append(starts, n)))
+    out = np.empty(n, dtype=out_dt)
+    out["electron"] = es
+    out["step_chan"] = (step.astype(np.uint32) << 5) | (head[order] & 15)
+    for name in out_dt.names[2:]:
+        out[name] = rec[name][order]
+    return out
 
 
 def launch(sim, mat, tables, bufs, block_size=0, stream=None):
@@ -244,12 +273,14 @@ def collect(bufs):
         events = bufs.ring[:k].cpu().numpy().view(event_dtype(bufs.ring_fields)).reshape(-1)
         if total > bufs.ring.shape[0]:
             status |= _lib.FLAG_RING_FULL
+        else:
+            events = unpack_events(events, bufs.ring_fields)
     return RunResult(tally, status, electrons, events, total)
 
 
 def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", electrons=True, ring_capacity=0,
         tally_channels=False, hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
-        J_scale=1.0, n_scale=1.0, block_size=0, device="cuda", tables=None):
+        J_scale=1.0, n_scale=1.0, block_size=0, device="cuda", tables=None, ring_fields=0):
     """Run one simulation to completion and return its results on the host."""
     _torch()
     p = with_defaults(input_par)
@@ -260,7 +291,7 @@ def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", elec
                    _lib.TALLY_CHANNELS if tally_channels else 0, J_scale, n_scale)
     if sim.mode == _lib.MODE_DS and tables is None:
         tables = ds_tables(mat, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"], device)
-    bufs = RunBuffers(n, prec, electrons, ring_capacity, device)
+    bufs = RunBuffers(n, prec, electrons, ring_capacity, device, ring_fields)
     bufs.zero()
     launch(sim, mat, tables if sim.mode == _lib.MODE_DS else None, bufs, block_size)
     return collect(bufs)

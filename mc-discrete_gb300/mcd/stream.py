@@ -7,9 +7,11 @@ of a simulation are cut into chunks; each chunk runs as one batched
 persistent launch whose every event is appended to a device ring
 (mcd_run_batched_ring), as a full 40-byte record or with only the fields a
 field mask selects (the scatter_output columns wanted; 8-byte header plus
-4 bytes per column).  Two rings alternate: while chunk c+1 is being
-transported, chunk c's records are copied to pinned host memory on a second
-stream, in pieces handed to a consumer callback.  A chunk whose events do
+4 bytes per column, or a 4-byte header with EV_PACKED_HEAD, whose records
+engine.unpack_events turns back into the 8-byte form chunk by chunk).  Two
+rings alternate: while chunk c+1 is being transported, chunk c's records
+are copied to pinned host memory on a second stream, in pieces handed to a
+consumer callback.  A chunk whose events do
 not fit its ring is re-run with a larger ring; the counter-based random
 stream makes the re-run exact.
 """

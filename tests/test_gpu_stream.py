@@ -89,3 +89,40 @@ def test_stream_of_selected_columns_equals_full_records(single):
     rec = key(rec)
     for f in ("electron", "step_chan", "W", "pathl", "c2", "x", "y", "z"):
         assert np.array_equal(rec[f], ref[f]), f
+
+
+def test_packed_header_stream_equals_full_records(single):
+    """With the one-word header (electron << 4 | channel) a record of step
+    length, W, cos^2(theta/2) and position is 28 bytes; the event index comes
+    back from the ring order of each electron's records."""
+    ref, _ = single
+    fields = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS | _lib.EV_PACKED_HEAD
+    es = EventStream(P, chunk=4000, seed=21, events_per_electron=450.0, tune=INLINE, fields=fields,
+                     piece_bytes=1 << 22)
+    chunks = {}
+
+    def consumer(rec, c):
+        chunks.setdefault(c, []).append(rec.copy())
+
+    stats = es.run(consumer)
+    assert es.rec_bytes == 28 and stats["bytes"] == stats["events"] * 28
+    parts = []
+    for c in sorted(chunks):
+        u = engine.unpack_events(np.concatenate(chunks[c]), fields)
+        u["electron"] += c * es.chunk
+        parts.append(u)
+    rec = key(np.concatenate(parts))
+    assert rec.size == ref.size
+    for f in ("electron", "step_chan", "W", "pathl", "c2", "x", "y", "z"):
+        assert np.array_equal(rec[f], ref[f]), f
+
+
+def test_packed_header_single_ring_equals_full_records(single):
+    ref, _ = single
+    fields = _lib.EV_ALL | _lib.EV_PACKED_HEAD
+    g = engine.run(P, num_el=P["num_el"], seed=21, precision="fp32", ring_capacity=P["num_el"] * 1500,
+                   ring_fields=fields)
+    rec = key(g.events)
+    assert rec.size == ref.size
+    for f in ("electron", "step_chan", "E", "W", "pathl", "c2", "half_phi", "x", "y", "z"):
+        assert np.array_equal(rec[f], ref[f]), f

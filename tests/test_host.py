@@ -195,14 +195,37 @@ def test_new_fields_are_validated_before_any_gpu_work():
     t = _lib.Tune(256, 0, 1, 0, 5)
     assert L.mcd_run_batched(C.cast(host, C.c_void_p), 1, C.cast(host, C.c_void_p), C.byref(t),
                              C.cast(host, C.c_void_p), None) == _lib.EINVAL
+    # ring field bits beyond the columns and the packed header
+    ring = _lib.EventRing(C.cast(host, C.c_void_p), 1, C.cast(host, C.c_void_p), 0x80, 0)
+    assert L.mcd_run_batched_ring(C.cast(host, C.c_void_p), 1, C.cast(host, C.c_void_p), None, C.byref(ring),
+                                  C.cast(host, C.c_void_p), None) == _lib.EINVAL
 
 
 def test_event_record_sizes_agree_with_library():
     from mcd import engine
     L = _lib.lib()
     assert L.mcd_event_bytes(0) == 40 == L.mcd_event_bytes(_lib.EV_ALL) == C.sizeof(_lib.Event)
-    for mask in range(64):
+    for mask in range(128):   # the columns, with and without the packed header
         assert engine.event_dtype(mask).itemsize == L.mcd_event_bytes(mask), mask
+    assert L.mcd_event_bytes(_lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS | _lib.EV_PACKED_HEAD) == 28
     cfg = _lib.EV_PATHL | _lib.EV_W | _lib.EV_C2 | _lib.EV_POS
     assert L.mcd_event_bytes(cfg) == 32
     assert engine.event_dtype(cfg).names == ("electron", "step_chan", "W", "pathl", "c2", "x", "y", "z")
+
+
+def test_packed_header_records_unpack_in_ring_order():
+    """The event index of a packed-header record is its rank among the
+    records of its electron in ring order."""
+    from mcd import engine
+    fields = _lib.EV_W | _lib.EV_PACKED_HEAD
+    dt = engine.event_dtype(fields)
+    assert dt.names == ("head", "W")
+    # three electrons interleaved in the ring; W = 10 * electron + event
+    ring = [(7, 0, 1), (2, 0, 0), (7, 1, 2), (5, 0, 3), (2, 1, 1), (7, 2, 0), (5, 1, 2)]
+    rec = np.array([((e << 4) | ch, 10.0 * e + k) for e, k, ch in ring], dtype=dt)
+    u = engine.unpack_events(rec, fields)
+    assert u.dtype.names == ("electron", "step_chan", "W")
+    assert list(u["electron"]) == [2, 2, 5, 5, 7, 7, 7]
+    assert list(u["step_chan"] >> 5) == [0, 1, 0, 1, 0, 1, 2]
+    assert np.array_equal(u["W"], 10.0 * u["electron"] + (u["step_chan"] >> 5))
+    assert list(u["step_chan"] & 31) == [0, 1, 3, 2, 1, 2, 0]
