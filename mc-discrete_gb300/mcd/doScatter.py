@@ -133,15 +133,19 @@ class NpzWriter:
 
 
 class HdfWriter:
-    """The reference's store layout through pandas.HDFStore (tables format)."""
+    """The reference's store layout through pandas.HDFStore: 'input' as the
+    one-row frame of the parameters (MC/doScatter.py:62-67), 'els' and
+    'scats' appended in tables format with data columns
+    (MC/doScatter.py:112-117).  String columns get room for the longest
+    label (the reference's 6 characters cut 'Gryz3s3p3d'), fixed when the
+    first chunk creates the table."""
 
     def __init__(self, name, inputPar):
         import pandas as pd
         self.pd = pd
         self.name = name
         self.store = pd.HDFStore(name, mode="w")
-        self.store["input"] = pd.Series([str(v) for v in inputPar.values()], index=list(inputPar.keys()),
-                                        dtype=str)
+        self.store["input"] = pd.DataFrame(pd.Series(inputPar)).T
         self.width = {"els": {"outcome": 6}, "scats": {"type": 24}}
 
     def append(self, key, cols):

@@ -55,3 +55,87 @@ def test_ring_fields_follow_requested_columns():
     assert doScatter.ring_fields(["energy"]) == _lib.EV_E | _lib.EV_W
     assert doScatter.ring_fields(list(doScatter.SCAT_COLS)) == _lib.EV_ALL
 
+
+class _Col:
+    def __init__(self, v):
+        self.v = np.asarray(v)
+
+    @property
+    def str(self):
+        return self
+
+    def len(self):
+        return _Col([len(x) for x in self.v])
+
+    def max(self):
+        return self.v.max() if self.v.size else 0
+
+
+class _Frame:
+    def __init__(self, data=None):
+        if isinstance(data, _Series):
+            self.cols = {0: data}
+        else:
+            self.cols = {k: np.asarray(v) for k, v in dict(data).items()}
+        self.transposed = False
+
+    @property
+    def T(self):
+        f = _Frame({})
+        f.cols = self.cols
+        f.transposed = not self.transposed
+        return f
+
+    def __contains__(self, c):
+        return c in self.cols
+
+    def __getitem__(self, c):
+        return _Col(self.cols[c])
+
+
+class _Series:
+    def __init__(self, d):
+        self.d = dict(d)
+
+
+class _Store:
+    def __init__(self, name, mode="a"):
+        self.name, self.mode = name, mode
+        self.items, self.puts, self.closed = {}, [], False
+
+    def __setitem__(self, k, v):
+        self.items[k] = v
+
+    def put(self, key, df, **kw):
+        self.puts.append((key, df, kw))
+
+    def close(self):
+        self.closed = True
+
+
+def test_hdf_writer_drives_pandas_like_the_reference(monkeypatch):
+    """The HDF5 branch (pandas and PyTables are absent here) against a
+    recording stand-in of the pandas calls the reference makes: the one-row
+    input frame (MC/doScatter.py:62-67) and tables-format appends with data
+    columns and string sizes (MC/doScatter.py:112-117)."""
+    import types
+    fake = types.ModuleType("pandas")
+    fake.HDFStore, fake.DataFrame, fake.Series = _Store, _Frame, _Series
+    monkeypatch.setitem(__import__("sys").modules, "pandas", fake)
+    p = config.with_defaults(dict(material="Au", mode="DS", E0=20000.0, Emin=1000.0, s_tilt=0.0,
+                                  tol_E=1e-3, tol_W=1e-3, electron_output=["outcome"], scatter_output=["type"]))
+    w = doScatter.HdfWriter("x.h5", p)
+    assert w.store.mode == "w"
+    inp = w.store.items["input"]
+    assert inp.transposed and inp.cols[0].d == p
+    w.append("els", {"outcome": np.array(["bks", "abs"]), "final_E": np.array([1.0, 2.0])})
+    w.append("scats", {"type": np.array(["Ruth", "Gryz3s3p3d"]), "E": np.array([1.0, 2.0])})
+    w.append("scats", {})
+    w.close()
+    assert w.store.closed
+    assert [k for k, _, _ in w.store.puts] == ["els", "scats"]
+    for key, df, kw in w.store.puts:
+        assert kw["format"] == "table" and kw["data_columns"] is True and kw["append"] is True
+    assert w.store.puts[0][2]["min_itemsize"] == {"outcome": 6}
+    assert w.store.puts[1][2]["min_itemsize"] == {"type": 24}
+    assert list(w.store.puts[1][1].cols["type"]) == ["Ruth", "Gryz3s3p3d"]
