@@ -51,6 +51,12 @@ BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
 # 1.3855e9 events); the issue peak is one warp instruction per scheduler
 # per cycle, 4 schedulers per SM
 WARP_INST_PER_EVENT = 14.82
+# the same capture's unit fractions (of peak sustained): issue-active cycles,
+# threads per warp instruction / 32, the L1/TEX unit, its shared-memory
+# wavefronts, and L2
+BATCHED_NCU = {"issue_active": 0.757, "warp_execution_efficiency": 0.717, "l1tex_throughput": 0.744,
+               "shared_wavefronts": 0.328, "l2_throughput": 0.017,
+               "capture": "ncu --set full of k_batched on a quarter of the workload (1.3855e9 events)"}
 
 
 def workload(scale=1.0):
@@ -662,6 +668,7 @@ def run_mcd(args):
                                "peak": sms * 4 * fmax / 1e9, "unit": "G warp instructions/s",
                                "frac": value * WARP_INST_PER_EVENT / ws / (sms * 4 * fmax),
                                "inst_per_event_note": "warp instructions per event from an ncu capture"},
+                     "ncu": BATCHED_NCU,
                      "peak_note": "nominal %d SMs x 128 FP32 lanes x 2 (MUFU: x16) at sm_max_mhz %.0f" % (sms, fmax / 1e6)},
         "cpu_baseline": {"value": cpu_v, "unit": "events/s", "cores": cpu["threads"], "kind": "port",
                          "sample": "C oracle, min(num_el, %d) electrons of each sim (%d events)"
