@@ -237,8 +237,8 @@ def cfg1_bench(args, dev):
     same = float(np.mean((g.electrons["outcome"] == c["outcome"]) & (g.electrons["n_events"] == c["n_events"])))
     return {"workload": CFG1_WORKLOAD, "num_el": n, "events": ev, "gpu_ms": statistics.median(ms),
             "gpu_events_per_s": ev / statistics.median(ms) * 1e3, "gpu_fp32_ms": statistics.median(ms32),
-            "note": "1000 electrons make 32 one-warp blocks on 32 of the SMs: the launch lasts as long as its "
-                    "longest trajectory, and FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU",
+            "note": "1000 electrons make 125 blocks of 8 threads: the launch lasts as long as its longest "
+                    "trajectory, and FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU",
             "cpu_1core_s": cpu[1], "cpu_all_cores_s": cpu[os.cpu_count() or 1], "cpu_cores": os.cpu_count() or 1,
             "eta_gpu_fp64": g.tally["bks"] / n, "eta_oracle": float(np.mean(c["outcome"] == 1)),
             "identical_trajectories": same, "gpu_launches": 2 * max(3, args.steps)}

@@ -268,9 +268,10 @@ int mcd_build_table(int kind, const mcd_material* mat, int shell,
  * (MC/tools/singleScatter.py:10-41, 205-239).  moller/gryz are used in DS
  * mode only (gryz = the outermost shell's table, which samples every
  * Gryzinski loss, MC/tools/scattering.py:625).  electrons and ring may be
- * NULL.  tally and status are device pointers.  block_size is a multiple of
- * 32 up to 256, or 0: 128, halved down to 32 while the grid would leave SMs
- * idle (results do not depend on it).                                      */
+ * NULL.  tally and status are device pointers.  block_size is 8, 16 or a
+ * multiple of 32 up to 256, or 0: 128, halved down to 8 while the grid would
+ * leave SMs idle, so that a small job spreads over more SMs with fewer
+ * lanes each (results do not depend on it).                                */
 int mcd_run(const mcd_sim* sim, const mcd_material* mat,
             const mcd_table* moller, const mcd_table* gryz,
             mcd_tally* tally, const mcd_electron_out* electrons,

@@ -1,9 +1,9 @@
 """Edge cases of the transport entry points: empty simulations alone and
 mixed into a batch, the largest batch (256 simulations), the event limit
 ('long' rows), a film thin enough that every electron is transmitted on
-its first step, a beam barely above Emin, and electron indices above 2^32
-(the Philox counter's high word), each against the oracle or the plain
-kernel."""
+its first step, a beam barely above Emin, electron indices above 2^32
+(the Philox counter's high word) and the plain kernel's block sizes, each
+against the oracle or the plain kernel."""
 import numpy as np
 import pytest
 
@@ -118,3 +118,18 @@ def test_electron_indices_above_two_to_the_32():
     g0 = engine.run(SI, num_el=300, seed=8, precision="fp64", first_electron=0)
     # a different counter range draws different electrons
     assert not np.array_equal(g.electrons["n_events"], g0.electrons["n_events"])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_block_size_does_not_change_results(prec):
+    """Blocks of 8 and 16 threads (what a small job gets automatically) give
+    the trajectories of full-warp blocks; other sizes are rejected."""
+    runs = [engine.run(SI, num_el=300, seed=4, precision=prec, block_size=b) for b in (8, 16, 32, 128, 0)]
+    for g in runs[1:]:
+        for k in INT_KEYS:
+            assert g.tally[k] == runs[0].tally[k], k
+        assert np.array_equal(g.electrons["n_events"], runs[0].electrons["n_events"])
+        assert np.array_equal(g.electrons["final_E"], runs[0].electrons["final_E"])
+    for b in (4, 24, 48, 512):
+        with pytest.raises(_lib.MCDError):
+            engine.run(SI, num_el=10, seed=4, precision=prec, block_size=b)
