@@ -11,10 +11,11 @@ expands to dx/dy/dz, 'position' to x/y/z, 'last_pos' to last_x/last_y/last_z.
 An electron that leaves through the surface and falls below Emin in the same
 step gets the reference's second 'abs' row (MC/tools/electron.py:52-54).
 
-The work runs on the GPU; `material` and `tables` may be the reference's
-objects (only their presence is checked) or None.  Each call takes a fresh
-range of Philox electron indices, so repeated calls give new trajectories;
-pass `seed` in inputPar to choose the stream.
+The work runs on the GPU.  `material` and `tables` keep the reference's
+signatures and are not used: the material comes from inputPar['material']
+and the tables are built on the GPU once per parameter set.  Each call
+takes a fresh range of Philox electron indices, so repeated calls give new
+trajectories; pass `seed` in inputPar to choose the stream.
 """
 import itertools
 import threading
@@ -23,11 +24,9 @@ import numpy as np
 
 from . import _lib
 from .config import with_defaults
+from .doScatter import EL_COLS, SCAT_COLS, ring_fields, type_labels
 from .engine import collect, launch, make_sim, mode_of, RunBuffers
 from .tables import ds_tables
-
-EL_COLS = ("outcome", "final_E", "final_dir", "last_pos")
-SCAT_COLS = ("type", "E", "E_loss", "pol_angle", "az_angle", "pathl", "position", "energy")
 
 _counter = itertools.count()
 _lock = threading.Lock()
@@ -37,16 +36,6 @@ def _next_range(n):
     with _lock:
         k = next(_counter)
     return k * (1 << 32), n
-
-
-def _type_names(mat, mode, elastic):
-    if mode == _lib.MODE_CONT:
-        return None
-    names = ["Ruth", "Moller", "Quinn"]
-    for k in range(mat.n_shells):
-        names.append("Gryz" + mat.shell_name[k].value.decode())
-    names += [""] * (_lib.CH_DIFF - len(names)) + ["diff"]
-    return names
 
 
 def _assemble(res, n, wanted, mat, mode, elastic):
@@ -59,7 +48,7 @@ def _assemble(res, n, wanted, mat, mode, elastic):
         if c not in SCAT_COLS:
             raise ValueError("scatter_output column %r is not produced (have %s)" % (c, SCAT_COLS))
     e = res.electrons
-    names = _type_names(mat, mode, elastic)
+    names = type_labels(mat, mode, elastic)
     ev = res.events
     order = np.lexsort((ev["step_chan"] >> 5, ev["electron"])) if ev is not None and ev.size else None
     if order is not None:
@@ -90,8 +79,7 @@ def _assemble(res, n, wanted, mat, mode, elastic):
             ch = (seg["step_chan"] & 31).astype(int)
             for c in sc_cols:
                 if c == "type":
-                    scats["type"] = ([names[k] for k in ch] if names is not None
-                                     else [elastic] * len(seg))
+                    scats["type"] = names[ch].tolist()
                 elif c == "E":
                     scats["E"] = seg["E"].astype(float).tolist()
                 elif c == "E_loss":
@@ -122,7 +110,6 @@ def _run_traj(inputPar, numTraj, thingsToSave):
     want_events = bool(thingsToSave.get("scat_output"))
     cap = n * 2048 if want_events else 0
     # the ring records carry only the requested scatter_output columns
-    from .doScatter import ring_fields
     fields = ring_fields(list(thingsToSave.get("scat_output", [])))
     while True:
         bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=fields)
