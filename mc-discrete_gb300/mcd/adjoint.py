@@ -16,8 +16,8 @@ mean ionisation energy J and the density, both as multipliers of the
 reference values (J_scale, n_scale), with the random numbers and the event
 sequence frozen.
 
-ExitHistogram.apply(J_scale, n_scale, model) wraps it as a torch.autograd
-Function.
+exit_histogram(J_scale, n_scale, model) wraps it as a torch.autograd
+Function of the two scale factors.
 """
 import ctypes as C
 
@@ -134,13 +134,14 @@ def _function():
     torch = _torch()
 
     class ExitHistogram(torch.autograd.Function):
-        """(J_scale, n_scale) -> (soft exit-energy bins [nbins], mean exit energy)."""
+        """(J_scale, n_scale) -> (soft bins [nbins], mean) of the model's quantity."""
 
         @staticmethod
         def forward(ctx, J_scale, n_scale, model):
             h, s, nb = model.forward(float(J_scale), float(n_scale))
             ctx.model = model
             ctx.nbks = max(nb, 1.0)
+            ctx.devs = (J_scale.device, n_scale.device)
             dev = J_scale.device
             return (torch.as_tensor(h, dtype=torch.float64, device=dev),
                     torch.as_tensor(s / ctx.nbks, dtype=torch.float64, device=dev))
@@ -150,7 +151,8 @@ def _function():
             gh = grad_h.detach().cpu().numpy() if grad_h is not None else np.zeros(ctx.model.nbins)
             gm = float(grad_m) if grad_m is not None else 0.0
             dJ, dn = ctx.model.backward(gh, gm / ctx.nbks)
-            return (torch.as_tensor(dJ, dtype=torch.float64), torch.as_tensor(dn, dtype=torch.float64), None)
+            return (torch.as_tensor(dJ, dtype=torch.float64, device=ctx.devs[0]),
+                    torch.as_tensor(dn, dtype=torch.float64, device=ctx.devs[1]), None)
 
     return ExitHistogram
 
@@ -159,7 +161,9 @@ _FN = None
 
 
 def exit_histogram(J_scale, n_scale, model):
-    """Differentiable (h, mean exit energy) for torch scalars J_scale, n_scale."""
+    """Differentiable (soft bins, mean) of the model's quantity (exit energy
+    or deepest z of the backscattered electrons) for torch scalars J_scale,
+    n_scale."""
     global _FN
     if _FN is None:
         _FN = _function()
