@@ -7,6 +7,8 @@ only exchange is one sum of the integer/FP64 tallies at the end.
 """
 import numpy as np
 
+from . import _lib
+
 INT_KEYS = ("none", "bks", "abs", "trsm", "trdf", "long", "events", "double_rows", "nan_events",
             "clamped", "long_path", "table_range")
 SUM_KEYS = ("sum_E_bks", "sum_E2_bks", "sum_steps2")
@@ -49,7 +51,7 @@ def tally_from_vector(v, sums=None):
     v = np.asarray(v, dtype=np.int64)
     out = {k: int(v[i]) for i, k in enumerate(INT_KEYS)}
     o = len(INT_KEYS)
-    for k, n in zip(ARRAY_KEYS, (16, 256, 180)):
+    for k, n in zip(ARRAY_KEYS, (_lib.MAX_CHANNELS, _lib.HIST_E_MAX, _lib.HIST_T_MAX)):
         out[k] = v[o:o + n].copy()
         o += n
     for k in SUM_KEYS:
