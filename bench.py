@@ -498,13 +498,18 @@ def run_mcd(args):
     else:
         tune, tune_table = autotune.tune(batch)
     graph = autotune.BatchGraph(batch, tune)
-    # plain path: one buffer set per simulation, no per-electron output
-    plain = []
+    # plain path: one launch and buffer set per simulation, no per-electron
+    # output; with a cross-section table per simulation (as the batched
+    # kernel reads) and with the cross sections evaluated inline
+    plain, plain_inline = [], []
     for k, s in enumerate(sims):
         mat = _lib.material(s["material"])
+        tabs = batch.tables[2 * (k // len(TILTS)): 2 * (k // len(TILTS)) + 2]
         sim = engine.make_sim(s, s["num_el"], args.seed, first, _lib.FP32, k)
-        bufs = engine.RunBuffers(s["num_el"], _lib.FP32, False, 0, dev)
-        plain.append((sim, mat, batch.tables[2 * (k // len(TILTS)): 2 * (k // len(TILTS)) + 2], bufs))
+        engine.use_sigma_table(sim, mat, dev)
+        plain.append((sim, mat, tabs, engine.RunBuffers(s["num_el"], _lib.FP32, False, 0, dev)))
+        sim = engine.make_sim(s, s["num_el"], args.seed, first, _lib.FP32, k)
+        plain_inline.append((sim, mat, tabs, engine.RunBuffers(s["num_el"], _lib.FP32, False, 0, dev)))
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
@@ -512,10 +517,13 @@ def run_mcd(args):
     def batched_step():                   # zero tallies, reset queue, launch: one graph
         graph.replay()
 
-    def plain_step():
-        for sim, mat, tabs, bufs in plain:
+    def plain_step(arm=plain):
+        for sim, mat, tabs, bufs in arm:
             bufs.zero()
             engine.launch(sim, mat, tabs, bufs, block_size=args.plain_block)
+
+    def plain_inline_step():
+        plain_step(plain_inline)
 
     def timed(step, k):
         total = 0.0
@@ -540,6 +548,7 @@ def run_mcd(args):
         batched_step()
         if not args.no_plain:
             plain_step()
+            plain_inline_step()
     torch.cuda.synchronize(dev)
     tallies, status = batch.collect()
     events = sum(t["events"] for t in tallies)
@@ -553,10 +562,11 @@ def run_mcd(args):
     clk = clocks.stop()
     k_plain = max(1, args.steps // 2)
     if args.no_plain:
-        t_plain, ptallies = float("nan"), tallies
+        t_plain, t_plain_inline, ptallies = float("nan"), float("nan"), tallies
     else:
         t_plain = timed(plain_step, k_plain)
         ptallies = [engine.collect(b[3]).tally for b in plain]
+        t_plain_inline = timed(plain_inline_step, k_plain)
     barrier()
 
     # end to end through the public API: host-side inputs packed and copied
@@ -577,9 +587,9 @@ def run_mcd(args):
     assert sum(t["events"] for t in e2e_tallies) == events
 
     if dist is not None:
-        tt = torch.tensor([t_batched, t_plain, t_e2e], dtype=torch.float64, device=dev)
+        tt = torch.tensor([t_batched, t_plain, t_plain_inline, t_e2e], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_batched, t_plain, t_e2e = tt.tolist()
+        t_batched, t_plain, t_plain_inline, t_e2e = tt.tolist()
         dist.destroy_process_group()
     if rank != 0:
         return
@@ -587,6 +597,7 @@ def run_mcd(args):
     K = args.steps
     value = events * ws * K / t_batched
     plain_value = events * ws * k_plain / t_plain
+    plain_inline_value = events * ws * k_plain / t_plain_inline
     # eta: batched vs plain (same counters) and vs the reference's samples
     zs = []
     for t, p in zip(tallies, ptallies):
@@ -655,8 +666,12 @@ def run_mcd(args):
                    "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
         "electrons_per_s": electrons * ws * K / t_batched,
         "plain": {"value": plain_value, "unit": "events/s", "ms_per_step": 1e3 * t_plain / k_plain,
-                  "launches_per_step": len(sims)},
+                  "launches_per_step": len(sims), "cross_sections": "one table per simulation"},
+        "plain_inline": {"value": plain_inline_value, "unit": "events/s",
+                         "ms_per_step": 1e3 * t_plain_inline / k_plain, "launches_per_step": len(sims),
+                         "cross_sections": "evaluated per event"},
         "batched_over_plain": value / plain_value,
+        "batched_over_plain_inline": value / plain_inline_value,
         "eta": {"batched_vs_plain_max_z": max(zs), "vs_reference": ref, "vs_oracle_fp64": vs_oracle},
         "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": batch.ws_bytes,
                 "d2h_bytes_per_step": int(batch.tallies.numel())},

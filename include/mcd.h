@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 7
+#define MCD_ABI_VERSION 8
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -152,6 +152,12 @@ typedef struct mcd_sim {
                                 and crossing the bottom face on that step is
                                 'trdf' (MC/tools/scattering.py:510-548,658-668,
                                 MC/tools/electron.py:72-79); needs xip_g > 0 */
+    const float* sigma_table;/* DS, FP32: device table from
+                                mcd_build_sigma_table for this simulation,
+                                read by mcd_run and mcd_run_batched_noalloc
+                                instead of evaluating the channel cross
+                                sections (NULL: evaluate them);
+                                mcd_batch_prepare builds its own tables      */
 } mcd_sim;
 
 /* ---- per-simulation tallies (device, caller zeroes them) ----------------- */
@@ -261,6 +267,18 @@ int mcd_build_table(int kind, const mcd_material* mat, int shell,
                     int32_t nE, int32_t nW, const float* Es, const float* Ws,
                     float* cdf32, double* cdf64, int32_t* nvalid, uint16_t* guide,
                     void* stream);
+
+/* Cross-section table of one DS simulation, for mcd_sim.sigma_table: on a
+ * log2-E grid of 128 points per octave over [Emin, E0], E times the total
+ * channel cross section and E times the running sums in pick order (Ruth,
+ * Moller, Gryzinski shells), FP64 evaluation of the expressions of
+ * MC/tools/crossSections.py:37-284 stored as FP32 -- the table the batched
+ * path builds per group of simulations.  It depends on the material, Wc,
+ * the elastic model, n_scale, E0 and Emin.  table is device memory of
+ * mcd_sigma_table_bytes() bytes.                                            */
+size_t mcd_sigma_table_bytes(void);
+int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat,
+                          float* table, void* stream);
 
 /* One simulation, one GPU thread per electron, one launch.
  * Replaces multiTraj_DS / multiTraj_cont (MC/tools/multiScatter.py:66-116,
@@ -373,7 +391,9 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * first call on a device looks up that array's address (issue it before any
  * stream capture).  Calls share the array: calls that overlap on the GPU
  * race.  The simulations are packed on the host and copied in on `stream`;
- * tallies[nsims] (zeroed by the caller) and status are device pointers.    */
+ * tallies[nsims] (zeroed by the caller) and status are device pointers.
+ * Cross sections are evaluated inline unless a simulation carries a
+ * caller-built sigma_table.                                                 */
 #define MCD_STATIC_MAX_SIMS 64
 int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims,
                             const mcd_material* mats, const int32_t* sim_material,

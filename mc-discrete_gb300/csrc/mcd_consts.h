@@ -94,8 +94,8 @@ struct SimConst {
     int32_t hE, hT;
     T invWE, invWT;  // 1/bin width (eV, degrees)
     TableDev tab[2];   // [0] Moller (valence), [1] Gryzinski (outermost shell)
-    // cumulative channel cross sections tabulated on a log-E grid (batched
-    // kernel only; nullptr = evaluate inline).  Row i (of sig_rows, sig_S
+    // cumulative channel cross sections tabulated on a log-E grid (FP32 DS
+    // transport; nullptr = evaluate inline).  Row i (of sig_rows, sig_S
     // floats apart) holds, at E = 2^(sig_l0 + i / sig_inv), E times the
     // total, then E times the running sums over the channels in pick order
     // before the last: Ruth, Moller, Gryz[0..nsh-1] (sig_K = nsh + 3 columns;
@@ -120,6 +120,18 @@ __host__ __device__ __forceinline__ int bits_S(const C& c) { return (int)((c.bit
 constexpr int kSigRowsMax = 4096;      // grid points of a cross-section table, at most
 constexpr int kSigStride = 12;         // floats per row, at most (3 + MCD_MAX_SHELLS + 1)
 constexpr double kSigPerOctave = 128;  // grid density
+
+// The log2-E grid of a cross-section table over [lo, hi] (eV), slightly
+// widened so that both ends interpolate inside it.
+inline void sigma_grid(double lo, double hi, float* l0, float* inv, float* tmax, int32_t* rows) {
+    const double a = log2(lo * (1.0 - 1e-6)), b = log2(hi * (1.0 + 1e-6));
+    int r = (int)ceil((b - a) * kSigPerOctave) + 1;
+    r = r < 2 ? 2 : (r > kSigRowsMax ? kSigRowsMax : r);
+    *l0 = (float)a;
+    *inv = (float)((r - 1) / (b - a));
+    *tmax = (float)(r - 2) + 0.999f;
+    *rows = r;
+}
 
 // Host-side builder: precompute the constant block of one simulation.
 template <class T>
@@ -208,12 +220,17 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     TableDev z{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0.0f, 0.0f};
     c.tab[0] = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->guide, tm->nE, tm->nW, tm->E_first, tm->E_last} : z;
     c.tab[1] = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->guide, tg->nE, tg->nW, tg->E_first, tg->E_last} : z;
-    // no table until a batch shares one among the simulations it fits
+    // the caller's table (mcd_run), or none until a batch shares one among
+    // the simulations it fits
     c.sig = nullptr;
     c.sig_l0 = c.sig_inv = c.sig_tmax = 0.0f;
     c.sig_K = m.n_shells + 3;
     c.sig_S = (c.sig_K + 3) & ~3;
     c.sig_rows = 0;
+    if (s.sigma_table && s.mode == MCD_MODE_DS) {
+        c.sig = s.sigma_table;
+        sigma_grid(s.Emin, s.E0, &c.sig_l0, &c.sig_inv, &c.sig_tmax, &c.sig_rows);
+    }
     c.bits = (c.quirks & 7u) | (c.diff ? kBitDiff : 0u) | (c.mode == MCD_MODE_CONT ? kBitCont : 0u) |
              ((c.tally_flags & MCD_TALLY_CHANNELS) ? kBitChan : 0u) | (c.ruth_r2 ? kBitR2 : 0u) |
              ((uint32_t)c.sig_K << 8) | ((uint32_t)c.sig_S << 12);
@@ -228,6 +245,7 @@ inline int check_sim(const mcd_sim& s, const mcd_material& m, const mcd_table* t
     if (s.precision != MCD_FP32 && s.precision != MCD_FP64) return MCD_EINVAL;
     if (s.elastic < MCD_ELASTIC_RUTH || s.elastic > MCD_ELASTIC_NIGRAM_WDEFL) return MCD_EINVAL;
     if (s.diff_mfp && (s.mode != MCD_MODE_DS || !(m.xip_g > 0))) return MCD_EINVAL;
+    if (s.sigma_table && (s.mode != MCD_MODE_DS || s.precision != MCD_FP32)) return MCD_EINVAL;
     if (!(s.E0 > s.Emin) || !(s.Emin > 0)) return MCD_EINVAL;
     if (s.num_el < 0) return MCD_EINVAL;
     if (m.n_shells < 0 || m.n_shells > MCD_MAX_SHELLS || m.atnd <= 0) return MCD_EINVAL;

@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* 
     bt_zero(&bt, 1);
     __syncthreads();
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr bool kTab = sizeof(T) == 4;   // FP32 transport may read a cross-section table
     uint32_t st = 0;
     if (i < (uint64_t)c.num_el) {
         Lane<T> L;
@@ -145,7 +146,7 @@ __global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* 
         const bool chan = (c.tally_flags & MCD_TALLY_CHANNELS) != 0;
         while (L.outcome == MCD_OUT_NONE) {
             EventOut<T> ev;
-            const int ch = (MODE == MCD_MODE_DS) ? ds_event<T, REC>(L, c, elec, &ev)
+            const int ch = (MODE == MCD_MODE_DS) ? ds_event<T, REC>(L, c, elec, &ev, kTab && c.sig != nullptr)
                                                  : cont_event<T, REC>(L, c, elec, &ev);
             if (ch >= 0) {
                 if (REC) st |= ring_append(ring, (uint32_t)i, L.step, ev);
@@ -336,19 +337,13 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
 // point); a slot is built when its simulation leads a group sharing it.  The
 // exact FP64 expressions of the inline path, stored as FP32 E * running sums
 // in pick order.
-__global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long long)nsims * kSigRowsMax) return;
-    const int s = (int)(gid / kSigRowsMax), i = (int)(gid % kSigRowsMax);
-    const SimConst<float>& cf = reinterpret_cast<const SimConst<float>*>(ws + batch_consts_off(nsims))[s];
-    const float* slot = reinterpret_cast<const float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s);
-    if (cf.sig != slot || i >= cf.sig_rows) return;
-    const SimConst<double>& c = reinterpret_cast<const SimConst<double>*>(ws + batch_dconsts_off(nsims))[s];
-    float* row = reinterpret_cast<float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s) + (size_t)i * cf.sig_S;
-    const double E = exp2((double)cf.sig_l0 + (double)i / (double)cf.sig_inv);
+// Row i of a table on the grid (l0, inv): [E total, E running sums Ruth,
+// +Moller, +Gryz[k] ... (the sum through Quinn is the total)], padding
+// FLT_MAX: never below a target.
+__device__ __forceinline__ void sig_row(const SimConst<double>& c, float l0, float inv, int S, int i,
+                                        float* row) {
+    const double E = exp2((double)l0 + (double)i / (double)inv);
     const double invE = 1.0 / E;
-    // [E total, E running sums Ruth, +Moller, +Gryz[k] ... (the sum through
-    // Quinn is the total)], padding FLT_MAX: never below a target
     double cum = sig_ruth<double>(c, E);
     int col = 1;
     row[col++] = (float)(E * cum);
@@ -360,7 +355,27 @@ __global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
     }
     cum += sig_quinn<double>(c, E, invE);
     row[0] = (float)(E * cum);
-    for (; col < cf.sig_S; ++col) row[col] = 3.402823466e38f;
+    for (; col < S; ++col) row[col] = 3.402823466e38f;
+}
+
+__global__ void __launch_bounds__(256) k_sigtab(uint8_t* ws, int nsims) {
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long long)nsims * kSigRowsMax) return;
+    const int s = (int)(gid / kSigRowsMax), i = (int)(gid % kSigRowsMax);
+    const SimConst<float>& cf = reinterpret_cast<const SimConst<float>*>(ws + batch_consts_off(nsims))[s];
+    const float* slot = reinterpret_cast<const float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s);
+    if (cf.sig != slot || i >= cf.sig_rows) return;
+    const SimConst<double>& c = reinterpret_cast<const SimConst<double>*>(ws + batch_dconsts_off(nsims))[s];
+    float* row = reinterpret_cast<float*>(ws + batch_sig_off(nsims) + batch_sig_bytes() * s) + (size_t)i * cf.sig_S;
+    sig_row(c, cf.sig_l0, cf.sig_inv, cf.sig_S, i, row);
+}
+
+// The table of one simulation (mcd_build_sigma_table): one thread per row.
+__global__ void __launch_bounds__(256) k_sigtab_one(const SimConst<double> c, float l0, float inv, int rows,
+                                                     int S, float* table) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows) return;
+    sig_row(c, l0, inv, S, i, table + (size_t)i * S);
 }
 
 // Do two simulations have the same channel cross sections at every energy?
@@ -401,14 +416,14 @@ inline void share_sigma_tables(const mcd_sim* sims, int nsims, const SimConst<do
                 lo = fmin(lo, sims[j].Emin);
                 hi = fmax(hi, sims[j].E0);
             }
-        const double l0 = log2(lo * (1.0 - 1e-6)), l1 = log2(hi * (1.0 + 1e-6));
-        int rows = (int)ceil((l1 - l0) * kSigPerOctave) + 1;
-        rows = rows < 2 ? 2 : (rows > kSigRowsMax ? kSigRowsMax : rows);
+        float l0, inv, tmax;
+        int32_t rows;
+        sigma_grid(lo, hi, &l0, &inv, &tmax, &rows);
         for (int j = k; j < nsims; ++j)
             if (cs[j].sig == slot) {
-                cs[j].sig_l0 = (float)l0;
-                cs[j].sig_inv = (float)((rows - 1) / (l1 - l0));
-                cs[j].sig_tmax = (float)(rows - 2) + 0.999f;
+                cs[j].sig_l0 = l0;
+                cs[j].sig_inv = inv;
+                cs[j].sig_tmax = tmax;
                 cs[j].sig_rows = rows;
             }
     }
@@ -487,6 +502,23 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
                                       status, st);
     return dispatch_plain<float>(make_consts<float>(*sim, *mat, tm, tg), block_size, tally, eo, rg, rec, status,
                                  st);
+}
+
+extern "C" size_t mcd_sigma_table_bytes(void) { return batch_sig_bytes(); }
+
+extern "C" int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat, float* table, void* stream) {
+    if (!sim || !mat || !table) return MCD_EINVAL;
+    if (sim->mode != MCD_MODE_DS) return MCD_EINVAL;
+    if (sim->elastic < MCD_ELASTIC_RUTH || sim->elastic > MCD_ELASTIC_NIGRAM_WDEFL) return MCD_EINVAL;
+    if (!(sim->E0 > sim->Emin) || !(sim->Emin > 0) || !(sim->Wc > 0)) return MCD_EINVAL;
+    if (mat->n_shells < 0 || mat->n_shells > MCD_MAX_SHELLS || mat->atnd <= 0) return MCD_EINVAL;
+    if ((reinterpret_cast<uintptr_t>(table) & 15) != 0) return MCD_EINVAL;   // rows are read as float4
+    mcd_sim s = *sim;
+    s.sigma_table = table;
+    const SimConst<double> c = make_consts<double>(s, *mat, nullptr, nullptr);
+    k_sigtab_one<<<(c.sig_rows + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        c, c.sig_l0, c.sig_inv, c.sig_rows, c.sig_S, table);
+    return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 
 extern "C" size_t mcd_batch_workspace_bytes(int32_t nsims) {

@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 7
+ABI_VERSION = 8
 MAX_SHELLS = 8
 GUIDE = 256
 MAX_CHANNELS = 16
@@ -110,6 +110,7 @@ class Sim(C.Structure):
         ("n_scale", C.c_double),
         ("elastic", C.c_int32),
         ("diff_mfp", C.c_int32),
+        ("sigma_table", C.c_void_p),
     ]
 
 
@@ -215,6 +216,8 @@ SIGNATURES = {
     "mcd_run": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.POINTER(Table), C.POINTER(Table),
                           C.c_void_p, C.POINTER(ElectronOut), C.POINTER(EventRing), C.c_void_p,
                           C.c_int32, C.c_void_p]),
+    "mcd_sigma_table_bytes": (C.c_size_t, []),
+    "mcd_build_sigma_table": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.c_void_p, C.c_void_p]),
     "mcd_batch_workspace_bytes": (C.c_size_t, [C.c_int32]),
     "mcd_batch_prepare": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
                                     C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),

@@ -27,7 +27,7 @@ import numpy as np
 
 from . import _lib
 from .config import readInput, with_defaults
-from .engine import collect, launch, make_sim, mode_of, RunBuffers
+from .engine import collect, launch, make_sim, mode_of, RunBuffers, use_sigma_table
 from .tables import ds_tables
 
 EL_COLS = ("outcome", "final_E", "final_dir", "last_pos")
@@ -198,6 +198,7 @@ def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_e
     while first < total:
         n = min(int(chunk), total - first)
         sim = make_sim(p, n, seed, first)
+        use_sigma_table(sim, mat)
         cap = int(1.3 * epe * n) + 4096 if sc_cols else 0
         while True:
             bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=ring_fields(sc_cols))

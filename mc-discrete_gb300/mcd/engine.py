@@ -12,7 +12,7 @@ import numpy as np
 
 from . import _lib
 from .config import with_defaults
-from .tables import ds_tables
+from .tables import ds_tables, sigma_table
 
 DEFAULT_HIST_E = (200, 100.0)   # 200 bins of 100 eV
 DEFAULT_HIST_T = (90, 1.0)      # 90 bins of 1 degree
@@ -102,6 +102,18 @@ def make_sim(input_par, num_el, seed=0, first_electron=0, precision=_lib.FP32, s
             raise KeyError("xip_g")
         s.diff_mfp = 1
     return s
+
+
+def use_sigma_table(sim, mat, device="cuda"):
+    """Point a DS FP32 simulation at its cross-section table (built once per
+    parameter set and kept alive by the cache); returns the table, or None
+    when the simulation evaluates its cross sections inline (continuous mode,
+    FP64 transport)."""
+    if sim.mode != _lib.MODE_DS or sim.precision != _lib.FP32:
+        return None
+    t = sigma_table(sim, mat, device)
+    sim.sigma_table = t.data_ptr()
+    return t
 
 
 def tally_to_dict(t):
@@ -280,8 +292,10 @@ def collect(bufs):
 
 def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", electrons=True, ring_capacity=0,
         tally_channels=False, hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
-        J_scale=1.0, n_scale=1.0, block_size=0, device="cuda", tables=None, ring_fields=0):
-    """Run one simulation to completion and return its results on the host."""
+        J_scale=1.0, n_scale=1.0, block_size=0, device="cuda", tables=None, ring_fields=0, tabulated=False):
+    """Run one simulation to completion and return its results on the host.
+    tabulated: DS FP32 transport reads the channel cross sections from a
+    table (use_sigma_table) instead of evaluating them."""
     _torch()
     p = with_defaults(input_par)
     n = int(p["num_el"] if num_el is None else num_el)
@@ -291,6 +305,8 @@ def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", elec
                    _lib.TALLY_CHANNELS if tally_channels else 0, J_scale, n_scale)
     if sim.mode == _lib.MODE_DS and tables is None:
         tables = ds_tables(mat, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"], device)
+    if tabulated:
+        use_sigma_table(sim, mat, device)
     bufs = RunBuffers(n, prec, electrons, ring_capacity, device, ring_fields)
     bufs.zero()
     launch(sim, mat, tables if sim.mode == _lib.MODE_DS else None, bufs, block_size)

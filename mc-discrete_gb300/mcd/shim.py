@@ -25,7 +25,7 @@ import numpy as np
 from . import _lib
 from .config import with_defaults
 from .doScatter import EL_COLS, SCAT_COLS, ring_fields, type_labels
-from .engine import collect, launch, make_sim, mode_of, RunBuffers
+from .engine import collect, launch, make_sim, mode_of, RunBuffers, use_sigma_table
 from .tables import ds_tables
 
 _counter = itertools.count()
@@ -105,6 +105,7 @@ def _run_traj(inputPar, numTraj, thingsToSave):
     first, n = _next_range(int(numTraj))
     seed = int(p.get("seed", 0))
     sim = make_sim(p, n, seed, first)
+    use_sigma_table(sim, mat)
     tables = (ds_tables(mat, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"])
               if mode == _lib.MODE_DS else None)
     want_events = bool(thingsToSave.get("scat_output"))

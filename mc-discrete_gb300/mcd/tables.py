@@ -256,3 +256,24 @@ def ds_tables(mat, E0, Emin, Wc, tol_E, tol_W, device="cuda"):
         t = (DeviceTable("Moller", mat, Wm, Em, device), DeviceTable("Gryz", mat, Wg, Eg, device))
         _CACHE[key] = t
     return t
+
+
+_SIG_CACHE = {}
+
+
+def sigma_table(sim, mat, device="cuda"):
+    """Device cross-section table of a DS simulation (mcd_build_sigma_table:
+    E times the total and running channel cross sections on a log2-E grid
+    over [Emin, E0]), cached per material, Wc, elastic model, density scale
+    and energy range."""
+    import torch
+    key = (bytes(mat), int(sim.elastic), float(sim.Wc), float(sim.n_scale), float(sim.E0), float(sim.Emin),
+           str(device))
+    t = _SIG_CACHE.get(key)
+    if t is None:
+        t = torch.empty(_lib.lib().mcd_sigma_table_bytes() // 4, dtype=torch.float32, device=device)
+        st = torch.cuda.current_stream(t.device)
+        code = _lib.lib().mcd_build_sigma_table(_lib.C.byref(sim), _lib.C.byref(mat), t.data_ptr(), st.cuda_stream)
+        _lib.check("mcd_build_sigma_table", code)
+        _SIG_CACHE[key] = t
+    return t

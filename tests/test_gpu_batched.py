@@ -5,7 +5,9 @@ on the same Philox counters (sim id, electron, event), so the integer tallies
 must agree; the refill setting only changes which lane runs which electron,
 never the result.  The default tabulated cross sections differ from the
 inline ones by at most 3e-7 relative, which moves a handful of trajectories:
-their tallies are checked against the inline ones within that allowance."""
+their tallies are checked against the inline ones within that allowance,
+and a plain launch reading the same table (mcd_sim.sigma_table) matches
+the batched kernel exactly."""
 import numpy as np
 import pytest
 
@@ -29,10 +31,12 @@ INT_KEYS = ("none", "bks", "abs", "trsm", "trdf", "long", "events", "double_rows
             "clamped", "long_path", "table_range")
 
 
-def plain(k, p):
+def plain(k, p, tabulated=False):
     # the batched kernel uses sim id = index in the batch; match it here
     mat = _lib.material(p["material"])
     sim = engine.make_sim(p, p["num_el"], seed=42, sim_id=k)
+    if tabulated:
+        engine.use_sigma_table(sim, mat)
     tabs = None
     if engine.mode_of(p) == _lib.MODE_DS:
         from mcd.tables import ds_tables
@@ -61,6 +65,21 @@ def test_batched_equals_plain(plain_tallies, refill, block, variant):
         assert np.array_equal(t["hist_T"], ref["hist_T"])
         assert abs(t["sum_E_bks"] - ref["sum_E_bks"]) <= 1e-9 * max(1.0, ref["sum_E_bks"])
         assert sum(t[o] for o in ("bks", "abs", "trsm", "trdf", "long")) == SIMS[k]["num_el"]
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_plain_with_its_table_equals_batched(variant):
+    """mcd_build_sigma_table builds the table the batched path builds for a
+    simulation whose group spans its own energy range (true of every DS
+    simulation here), so a plain launch reading it runs the batched
+    kernel's trajectories."""
+    b = engine.Batch(SIMS, seed=42)
+    res, status = b.run(_lib.Tune(256, 0, 1, variant, 0))
+    for k, p in enumerate(SIMS):
+        ref = plain(k, p, tabulated=True)
+        for key in INT_KEYS:
+            assert res[k][key] == ref[key], (k, key, res[k][key], ref[key])
+        assert np.array_equal(res[k]["hist_E"], ref["hist_E"])
 
 
 @pytest.mark.parametrize("variant", [0, 1])

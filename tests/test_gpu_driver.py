@@ -39,7 +39,8 @@ def test_cli_writes_reference_tables(tmp_path):
     z = np.load(name)
     assert str(z["input/material"]) == "Si" and str(z["input/num_el"]) == "3000"
     oc = z["els/outcome"]
-    g = engine.run(p, num_el=3000, seed=0)          # the same electrons: indices 0..2999, seed 0
+    # the same electrons (indices 0..2999, seed 0) with the same cross-section table
+    g = engine.run(p, num_el=3000, seed=0, tabulated=True)
     t = g.tally
     assert (oc == "bks").sum() == t["bks"] and (oc == "abs").sum() == t["abs"] + t["double_rows"]
     assert oc.size == 3000 + t["double_rows"]

@@ -39,7 +39,7 @@ def test_struct_layouts_match():
 
 def test_abi_and_errors():
     L = _lib.lib()
-    assert L.mcd_abi_version() == _lib.ABI_VERSION == 7
+    assert L.mcd_abi_version() == _lib.ABI_VERSION == 8
     assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
     m = _lib.Material()
     assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
@@ -190,6 +190,12 @@ def test_new_fields_are_validated_before_any_gpu_work():
     assert L.mcd_adjoint_forward(C.byref(engine.make_sim(p, 16)), C.byref(mat), C.byref(h), C.byref(buf), 1, None,
                                  1, None) == _lib.EINVAL
     assert L.mcd_project_detector(None, 5, _lib.FP32, 20.0, 0.0, 0.0, 0.0, None, None) == _lib.EINVAL
+    # a cross-section table is for DS FP32 transport only
+    s = engine.make_sim(p, 16)                       # continuous mode
+    s.sigma_table = C.addressof(C.c_float(0.0))
+    assert L.mcd_run(C.byref(s), C.byref(mat), None, None, 1, None, None, 1, 128, None) == _lib.EINVAL
+    assert L.mcd_build_sigma_table(C.byref(s), C.byref(mat), None, None) == _lib.EINVAL
+    assert L.mcd_sigma_table_bytes() == 4 * 4096 * 12
     # the reserved tuning word must be zero (host buffers: nothing is dereferenced)
     host = (C.c_uint8 * 64)()
     t = _lib.Tune(256, 0, 1, 0, 5)
