@@ -213,8 +213,9 @@ def cfg1_bench(args, dev):
         torch.cuda.synchronize(dev)
         ms.append(e0.elapsed_time(e1))
     g = engine.collect(bufs)
-    # the same launch in FP32 transport
+    # the same launch in FP32 transport, with the simulation's cross-section table
     sim32 = engine.make_sim(p, n, seed=args.seed, precision=_lib.FP32)
+    engine.use_sigma_table(sim32, mat, dev)
     b32 = engine.RunBuffers(n, _lib.FP32, True, 0, device=dev)
     ms32 = []
     for k in range(args.warmup + max(3, args.steps)):
