@@ -239,3 +239,21 @@ def test_packed_header_records_unpack_in_ring_order():
     assert list(u["step_chan"] >> 5) == [0, 1, 0, 1, 0, 1, 2]
     assert np.array_equal(u["W"], 10.0 * u["electron"] + (u["step_chan"] >> 5))
     assert list(u["step_chan"] & 31) == [0, 1, 3, 2, 1, 2, 0]
+
+
+def test_c_caller_links_and_runs(tmp_path):
+    """The header compiles as strict C99 and a C program links against the
+    library and calls its host-only entry points (no GPU call)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = _lib.lib()._name
+    exe = str(tmp_path / "capi_check")
+    src = os.path.join(ROOT, "tests", "capi_check.c")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        src, lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok %d" % _lib.ABI_VERSION, (r.returncode, r.stdout)
