@@ -171,21 +171,37 @@ __device__ __forceinline__ int table_row(const TableDev& t, T E, bool* out_of_ra
 
 template <class T>
 __device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) {
-    const int i = table_row(t, E, oor);
     const int ncol = t.nW - 1;
-    const float* row = t.cdf + (size_t)i * ncol;
-    int lo, hi;
-    if (t.guide) {
-        // the answer lies between the first entries >= k/G and >= (k+1)/G,
-        // usually the same column (no CDF read at all)
-        const int k = (int)(U * (T)MCD_GUIDE);
-        const uint16_t* g = t.guide + (size_t)i * (MCD_GUIDE + 1) + k;
-        lo = __ldg(g);
-        hi = __ldg(g + 1);
-    } else {
-        lo = 0;
-        hi = t.nvalid ? __ldg(t.nvalid + i) : ncol;
+    const int kq = (int)(U * (T)MCD_GUIDE);
+    int i = -1, lo = 0, hi = 0;
+    if (t.guide && t.E_last > 0.0f && E > (T)t.E_first && !(E > (T)t.E_last)) {
+        // the row guess's bracketing energies and its guide entries in one
+        // round trip, kept when the guess is the row (as it usually is: the
+        // E grid is a float32 linspace); otherwise the search below
+        const int nE = t.nE;
+        int g = (int)ceil((E - (T)t.E_first) * (T)(nE - 1) / (T)(t.E_last - t.E_first));
+        g = g < 1 ? 1 : (g > nE - 1 ? nE - 1 : g);
+        const uint16_t* gp = t.guide + (size_t)g * (MCD_GUIDE + 1) + kq;
+        const T a = (T)__ldg(t.Es + g - 1), b = (T)__ldg(t.Es + g);
+        const int glo = __ldg(gp), ghi = __ldg(gp + 1);
+        if (a < E && E <= b) {
+            i = g;
+            lo = glo;
+            hi = ghi;
+        }
     }
+    if (i < 0) {
+        i = table_row(t, E, oor);
+        if (t.guide) {
+            const uint16_t* gp = t.guide + (size_t)i * (MCD_GUIDE + 1) + kq;
+            lo = __ldg(gp);
+            hi = __ldg(gp + 1);
+        } else {
+            lo = 0;
+            hi = t.nvalid ? __ldg(t.nvalid + i) : ncol;
+        }
+    }
+    const float* row = t.cdf + (size_t)i * ncol;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         const float v = __ldg(row + mid);
