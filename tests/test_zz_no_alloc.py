@@ -67,6 +67,19 @@ def test_noalloc_matches_workspace_run_twice():
         assert sum(t[o] for o in ("bks", "abs", "trsm", "long")) == s["num_el"]
 
 
+def test_noalloc_reads_caller_built_cross_section_tables():
+    """Simulations that carry a table from mcd_build_sigma_table run from it;
+    each DS simulation here is alone in its cross-section group, so the
+    workspace run's tables are the same tables and the tallies agree."""
+    b = engine.Batch(SIMS, seed=17)
+    ref, st_ref = b.run(_lib.Tune(256, 0, 1, 0, 0))
+    keep = [engine.use_sigma_table(b._sims_arr[k], b.mats[b._idx[0][k]]) for k in range(b.n)]
+    assert sum(t is not None for t in keep) == 3
+    got, st = _noalloc(b, _lib.Tune(256, 0, 1, 0, 0))
+    _same(got, ref)
+    assert st == st_ref
+
+
 def test_noalloc_rejects_too_many_simulations():
     b = engine.Batch(SIMS[:1], seed=1)
     n = _lib.STATIC_MAX_SIMS + 1
