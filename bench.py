@@ -674,7 +674,7 @@ def run_mcd(args):
         "batched_over_plain": value / plain_value,
         "batched_over_plain_inline": value / plain_inline_value,
         "eta": {"batched_vs_plain_max_z": max(zs), "vs_reference": ref, "vs_oracle_fp64": vs_oracle},
-        "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": batch.ws_bytes,
+        "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": int(_lib.lib().mcd_batch_upload_bytes(batch.n)),
                 "d2h_bytes_per_step": int(batch.tallies.numel())},
         "roofline": {"bound": "fp32-issue", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": ach / fp32_peak, "traffic": BATCHED_DRAM_BYTES if args.scale == 1.0 else None,

@@ -310,6 +310,9 @@ int mcd_run(const mcd_sim* sim, const mcd_material* mat,
  * Replaces MapScatterer.__call__ (MC/doScatter.py:54-95) with its pool of
  * multiTraj_* jobs.                                                          */
 size_t mcd_batch_workspace_bytes(int32_t nsims);
+/* Bytes mcd_batch_prepare copies from the host (the workspace less its
+ * table slots, which the GPU fills).                                        */
+size_t mcd_batch_upload_bytes(int32_t nsims);
 int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims,
                       const mcd_material* mats, const int32_t* sim_material,
                       const mcd_table* tables, const int32_t* sim_moller,

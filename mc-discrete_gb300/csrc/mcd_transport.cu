@@ -526,6 +526,11 @@ extern "C" size_t mcd_batch_workspace_bytes(int32_t nsims) {
     return batch_bytes(nsims);
 }
 
+extern "C" size_t mcd_batch_upload_bytes(int32_t nsims) {
+    if (nsims <= 0 || nsims > kBatchMaxSims) return 0;
+    return batch_sig_off(nsims);
+}
+
 extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_material* mats,
                                  const int32_t* sim_material, const mcd_table* tables, const int32_t* sim_moller,
                                  const int32_t* sim_gryz, void* workspace, size_t workspace_bytes, void* stream) {

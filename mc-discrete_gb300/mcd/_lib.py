@@ -219,6 +219,7 @@ SIGNATURES = {
     "mcd_sigma_table_bytes": (C.c_size_t, []),
     "mcd_build_sigma_table": (C.c_int, [C.POINTER(Sim), C.POINTER(Material), C.c_void_p, C.c_void_p]),
     "mcd_batch_workspace_bytes": (C.c_size_t, [C.c_int32]),
+    "mcd_batch_upload_bytes": (C.c_size_t, [C.c_int32]),
     "mcd_batch_prepare": (C.c_int, [C.POINTER(Sim), C.c_int32, C.POINTER(Material), C.POINTER(C.c_int32),
                                     C.POINTER(Table), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                     C.c_void_p, C.c_size_t, C.c_void_p]),

@@ -51,6 +51,9 @@ def test_entry_points_reject_bad_arguments_without_touching_the_gpu():
     assert L.mcd_run(None, None, None, None, None, None, None, None, 128, None) == _lib.EINVAL
     assert L.mcd_batch_workspace_bytes(0) == 0
     assert L.mcd_batch_workspace_bytes(257) == 0
+    assert L.mcd_batch_upload_bytes(0) == 0 and L.mcd_batch_upload_bytes(257) == 0
+    # the upload is the workspace less its 64 table slots (4096 x 12 floats each)
+    assert L.mcd_batch_upload_bytes(64) <= L.mcd_batch_workspace_bytes(64) - 64 * 4 * 4096 * 12
     assert L.mcd_build_table(0, None, 0, 1, 2, None, None, None, None, None, None, None) == _lib.EINVAL
     assert L.mcd_run_batched(None, 1, None, None, None, None) == _lib.EINVAL
 
