@@ -2,7 +2,8 @@
 
 tune(batch) times the kernel on a scaled-down copy of the batch (every
 simulation keeps its parameters; electron counts shrink) for each block size
-x refill granularity x register budget, and returns the fastest mcd_tune.  Results are cached
+x refill granularity x register budget, times the few fastest again on the
+batch itself, and returns the fastest mcd_tune.  Results are cached
 in a JSON file keyed by the GPU name and a signature of the workload, so a
 later process reuses them without timing.
 
@@ -73,8 +74,10 @@ def _time(batch, t, reps):
     return best
 
 
-def tune(batch, fraction=0.1, reps=2, use_cache=True, blocks=BLOCKS, refills=REFILLS):
-    """Fastest mcd_tune for `batch`; returns (tune, table of timings in ms)."""
+def tune(batch, fraction=0.1, reps=2, use_cache=True, blocks=BLOCKS, refills=REFILLS, finalists=3):
+    """Fastest mcd_tune for `batch`; returns (tune, table of timings in ms).
+    Every shape is timed on the scaled-down copy; the `finalists` fastest are
+    timed again on the batch itself, which decides."""
     key = signature(batch)
     db = _load() if use_cache else {}
     if key in db:
@@ -97,6 +100,14 @@ def tune(batch, fraction=0.1, reps=2, use_cache=True, blocks=BLOCKS, refills=REF
                     best = (ms, b, r, v)
     if best is None:
         raise RuntimeError("no launch shape fits the batched kernel")
+    if finalists > 1:
+        ranked = sorted(table.items(), key=lambda kv: kv[1])[:finalists]
+        full = []
+        for k, _ in ranked:
+            b, r, v = (int(x) for x in k.split("/"))
+            full.append((_time(batch, _lib.Tune(b, 0, r, v, 0), 3), b, r, v))
+            table["full:" + k] = full[-1][0]
+        best = min(full)
     db[key] = {"block": best[1], "refill": best[2], "variant": best[3], "table": table}
     if use_cache:
         _store(db)

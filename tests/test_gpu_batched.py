@@ -142,6 +142,10 @@ def test_autotune_picks_a_measured_shape(tmp_path, monkeypatch):
     b = engine.Batch(SIMS[:3], seed=4)
     t, table = autotune.tune(b, fraction=0.2, reps=1, blocks=(128, 256), refills=(1, 8))
     k = "%d/%d/%d" % (t.block_size, t.refill, t.variant)
-    assert k in table and min(table.values()) == table[k]
+    full = {key[5:]: ms for key, ms in table.items() if key.startswith("full:")}
+    scaled = {key: ms for key, ms in table.items() if not key.startswith("full:")}
+    # the finalists are the three fastest on the scaled copy; the batch itself decides
+    assert set(full) == set(sorted(scaled, key=scaled.get)[:3])
+    assert k in full and min(full.values()) == full[k]
     t2, _ = autotune.tune(b)          # from the cache
     assert (t2.block_size, t2.refill) == (t.block_size, t.refill)
