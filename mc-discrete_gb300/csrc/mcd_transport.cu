@@ -227,7 +227,7 @@ static void batch_order(const mcd_sim* sims, int nsims, int32_t* perm) {
     }
 }
 
-template <int MODE_MIX, bool REC, int MINB>
+template <bool REC>
 __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
                                              const mcd_event_ring& ring, int inline_sigma);
 
@@ -236,21 +236,22 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
 // 64-simulation workload), or 5 blocks of 256 per SM at 48 registers (40
 // warps, a few spilled values, and five copies of the constant blocks in
 // shared memory, which take L1 capacity).
-template <int MODE_MIX, bool REC = false>
+// REC: append every event to the ring.
+template <bool REC = false>
 __global__ void __launch_bounds__(1024) k_batched(uint8_t* ws, mcd_tally* tallies, int refill,
                                                   uint32_t* status, const mcd_event_ring ring = mcd_event_ring{},
                                                   int inline_sigma = 0) {
-    batched_body<MODE_MIX, REC, 0>(ws, tallies, refill, status, ring, inline_sigma);
+    batched_body<REC>(ws, tallies, refill, status, ring, inline_sigma);
 }
 
-template <int MODE_MIX, bool REC = false>
+template <bool REC = false>
 __global__ void __launch_bounds__(256, 5) k_batched_lr(uint8_t* ws, mcd_tally* tallies, int refill,
                                                        uint32_t* status, const mcd_event_ring ring = mcd_event_ring{},
                                                        int inline_sigma = 0) {
-    batched_body<MODE_MIX, REC, 1>(ws, tallies, refill, status, ring, inline_sigma);
+    batched_body<REC>(ws, tallies, refill, status, ring, inline_sigma);
 }
 
-template <int MODE_MIX, bool REC, int MINB>
+template <bool REC>
 __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, int refill, uint32_t* status,
                                              const mcd_event_ring& ring, int inline_sigma) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -316,7 +317,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
             const SimConst<float>& c = s_c[sim];
             EventOut<float> ev;
             int ch;
-            if (MODE_MIX == 0 || !(c.bits & kBitCont))
+            if (!(c.bits & kBitCont))
                 ch = ds_event<float, REC>(L, c, c.first + local, &ev, !inline_sigma && c.sig != nullptr);
             else
                 ch = cont_event<float, REC>(L, c, c.first + local, &ev);
@@ -608,7 +609,7 @@ extern "C" int mcd_run_batched(void* workspace, int32_t nsims, mcd_tally* tallie
     if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
     const size_t smem = batch_smem(nsims);
-    auto kern = lowreg ? k_batched_lr<1> : k_batched<1>;
+    auto kern = lowreg ? k_batched_lr<false> : k_batched<false>;
     if (smem > 48 * 1024) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return MCD_ECUDA;
@@ -647,18 +648,18 @@ extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* t
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
     const size_t smem = batch_smem(nsims);
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_batched<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaFuncSetAttribute(k_batched<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
         return MCD_ECUDA;
     int fit = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<1, true>, block, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<true>, block, smem) != cudaSuccess)
         return MCD_ECUDA;
     if (fit < 1) return MCD_ETOOBIG;
     if (per_sm <= 0 || per_sm > fit) per_sm = fit;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(workspace, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
     const int inline_sigma = (tune && (tune->variant & 2)) ? 1 : 0;
-    k_batched<1, true><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status,
+    k_batched<true><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(workspace), tallies, refill, status,
                                                           *ring, inline_sigma);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
@@ -768,10 +769,10 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
     const size_t smem = batch_smem(nsims);
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_batched<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        cudaFuncSetAttribute(k_batched<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return MCD_ECUDA;
     int fit = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<1>, block, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<false>, block, smem) != cudaSuccess)
         return MCD_ECUDA;
     if (fit < 1) return MCD_ETOOBIG;
     if (per_sm <= 0 || per_sm > fit) per_sm = fit;
@@ -779,6 +780,6 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     // pageable source: the call returns once `host` has been staged, so the
     // stack buffer may go out of scope afterwards
     if (cudaMemcpyAsync(scratch, host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) return MCD_ECUDA;
-    k_batched<1><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(scratch), tallies, refill, status);
+    k_batched<false><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(scratch), tallies, refill, status);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
