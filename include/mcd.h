@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 8
+#define MCD_ABI_VERSION 9
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -158,6 +158,12 @@ typedef struct mcd_sim {
                                 instead of evaluating the channel cross
                                 sections (NULL: evaluate them);
                                 mcd_batch_prepare builds its own tables      */
+    const struct mcd_electron_out* electrons;
+                             /* mcd_batch_prepare, mcd_run_batched_noalloc:
+                                this simulation's per-electron rows (device
+                                arrays for num_el electrons, FP32; NULL:
+                                none), read when the batch is packed; mcd_run
+                                takes its rows as an argument instead       */
 } mcd_sim;
 
 /* ---- per-simulation tallies (device, caller zeroes them) ----------------- */
@@ -389,7 +395,7 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * memory through its own arena; a caller for which an allocation, which can
  * synchronise the device, would break its latency budget).  No counterpart
  * in the reference.  Its scratch is a static device array sized for
- * MCD_STATIC_MAX_SIMS simulations (28.5 KiB), resident on every GPU that
+ * MCD_STATIC_MAX_SIMS simulations (32 KiB), resident on every GPU that
  * loads the library until exit; more simulations return MCD_ETOOBIG.  The
  * first call on a device looks up that array's address (issue it before any
  * stream capture).  Calls share the array: calls that overlap on the GPU

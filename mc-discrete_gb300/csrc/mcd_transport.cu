@@ -181,10 +181,24 @@ __host__ __device__ constexpr size_t batch_perm_off(int nsims) {
 __host__ __device__ constexpr size_t batch_consts_off(int nsims) {
     return (batch_perm_off(nsims) + sizeof(int32_t) * (size_t)nsims + 255) & ~(size_t)255;
 }
-// ... | FP64 constants (table build only) | cross-section tables.  The no-alloc
-// path copies only the core (up to the FP32 constants) and runs without tables.
-__host__ __device__ constexpr size_t batch_core_bytes(int nsims) {
+// ... | per-electron row pointers[nsims] | FP64 constants (table build only)
+// | cross-section tables.  The no-alloc path copies only the core (through
+// the row pointers) and has no table slots.
+__host__ __device__ constexpr size_t batch_elout_off(int nsims) {
     return batch_consts_off(nsims) + sizeof(SimConst<float>) * (size_t)nsims;
+}
+__host__ __device__ constexpr size_t batch_core_bytes(int nsims) {
+    return batch_elout_off(nsims) + sizeof(mcd_electron_out) * (size_t)nsims;
+}
+static_assert(sizeof(SimConst<float>) % 8 == 0, "row pointers follow the constant blocks");
+
+// The row pointers of each simulation (zero: none), as the kernel reads them.
+inline void pack_rows(const mcd_sim* sims, int nsims, uint8_t* host) {
+    mcd_electron_out* eo = reinterpret_cast<mcd_electron_out*>(host + batch_elout_off(nsims));
+    for (int k = 0; k < nsims; ++k) {
+        if (sims[k].electrons) eo[k] = *sims[k].electrons;
+        else memset(&eo[k], 0, sizeof(mcd_electron_out));
+    }
 }
 __host__ __device__ constexpr size_t batch_dconsts_off(int nsims) {
     return (batch_core_bytes(nsims) + 255) & ~(size_t)255;
@@ -286,7 +300,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
     bool have = false;
     bool exhausted = false;
     uint32_t st = 0;
-    const ElOut eo{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const mcd_electron_out* rows = reinterpret_cast<const mcd_electron_out*>(ws + batch_elout_off(nsims));
     while (true) {
         const unsigned idle = __ballot_sync(0xffffffffu, !have);
         if (!exhausted && idle && (__popc(idle) >= refill || idle == 0xffffffffu)) {
@@ -324,6 +338,8 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
             if (REC && ch >= 0) st |= ring_append(ring, (uint32_t)local, L.step, ev);
             if (ch >= 0 && (c.bits & kBitChan)) atomicAdd(&s_t[sim].channel[ch], 1u);
             if (L.outcome != MCD_OUT_NONE) {
+                const mcd_electron_out& r = rows[sim];
+                const ElOut eo{r.outcome, r.flags, r.final_E, r.dir, r.last_pos, r.max_z, r.n_events};
                 st |= finish_electron(c, L, local, s_t[sim], tallies + sim, eo);
                 have = false;
             }
@@ -566,6 +582,7 @@ extern "C" int mcd_batch_prepare(const mcd_sim* sims, int32_t nsims, const mcd_m
         cd[k] = make_consts<double>(s, m, tm, tg);
     }
     if (rc == MCD_OK) share_sigma_tables(sims, nsims, cd, cs, static_cast<const uint8_t*>(workspace));
+    if (rc == MCD_OK) pack_rows(sims, nsims, host);
     batch_order(sims, nsims, perm);
     unsigned long long acc = 0;
     for (int q = 0; q < nsims; ++q) {
@@ -759,7 +776,10 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     h->queue = 0;
     h->total = acc;
     h->nsims = nsims;
-    const size_t bytes = batch_core_bytes(nsims);   // no cross-section tables: sig stays null
+    pack_rows(sims, nsims, host);
+    // the core only: cross sections come from the callers' tables or are
+    // evaluated inline
+    const size_t bytes = batch_core_bytes(nsims);
 
     void* scratch = nullptr;
     int rc = static_scratch(&scratch);

@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 8
+ABI_VERSION = 9
 MAX_SHELLS = 8
 GUIDE = 256
 MAX_CHANNELS = 16
@@ -111,6 +111,7 @@ class Sim(C.Structure):
         ("elastic", C.c_int32),
         ("diff_mfp", C.c_int32),
         ("sigma_table", C.c_void_p),
+        ("electrons", C.c_void_p),   # host address of an ElectronOut (batched runs)
     ]
 
 

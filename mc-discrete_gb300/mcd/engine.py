@@ -134,6 +134,34 @@ def tally_from_bytes(buf):
     return tally_to_dict(t)
 
 
+def _device_rows(n, fdt, device):
+    """Per-electron row arrays on the device (the mcd_electron_out layout)."""
+    torch = _torch()
+    return dict(
+        outcome=torch.zeros(n, dtype=torch.uint8, device=device),
+        flags=torch.zeros(n, dtype=torch.uint8, device=device),
+        final_E=torch.zeros(n, dtype=fdt, device=device),
+        dir=torch.zeros(3 * n, dtype=fdt, device=device),
+        last_pos=torch.zeros(3 * n, dtype=fdt, device=device),
+        max_z=torch.zeros(n, dtype=fdt, device=device),
+        n_events=torch.zeros(n, dtype=torch.int32, device=device),
+    )
+
+
+def _rows_struct(e):
+    return _lib.ElectronOut(e["outcome"].data_ptr(), e["flags"].data_ptr(), e["final_E"].data_ptr(),
+                            e["dir"].data_ptr(), e["last_pos"].data_ptr(), e["max_z"].data_ptr(),
+                            e["n_events"].data_ptr())
+
+
+def _host_rows(el, n):
+    """Per-electron rows copied to the host (dir and last_pos as (n, 3))."""
+    e = {k: v.cpu().numpy() for k, v in el.items()}
+    return dict(outcome=e["outcome"], flags=e["flags"], final_E=e["final_E"],
+                dir=e["dir"].reshape(3, n).T.copy(), last_pos=e["last_pos"].reshape(3, n).T.copy(),
+                max_z=e["max_z"], n_events=e["n_events"])
+
+
 class RunBuffers:
     """Device buffers of one simulation (re-usable across launches)."""
 
@@ -146,18 +174,7 @@ class RunBuffers:
         self.tally = torch.zeros(tsz, dtype=torch.uint8, device=self.device)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         fdt = torch.float32 if precision == _lib.FP32 else torch.float64
-        self.el = None
-        if electrons:
-            n = self.num_el
-            self.el = dict(
-                outcome=torch.zeros(n, dtype=torch.uint8, device=self.device),
-                flags=torch.zeros(n, dtype=torch.uint8, device=self.device),
-                final_E=torch.zeros(n, dtype=fdt, device=self.device),
-                dir=torch.zeros(3 * n, dtype=fdt, device=self.device),
-                last_pos=torch.zeros(3 * n, dtype=fdt, device=self.device),
-                max_z=torch.zeros(n, dtype=fdt, device=self.device),
-                n_events=torch.zeros(n, dtype=torch.int32, device=self.device),
-            )
+        self.el = _device_rows(self.num_el, fdt, self.device) if electrons else None
         self.ring = None
         self.ring_fields = int(ring_fields)
         if ring_capacity:
@@ -172,12 +189,7 @@ class RunBuffers:
             self.cursor.zero_()
 
     def electron_struct(self):
-        if self.el is None:
-            return None
-        e = self.el
-        return _lib.ElectronOut(e["outcome"].data_ptr(), e["flags"].data_ptr(), e["final_E"].data_ptr(),
-                                e["dir"].data_ptr(), e["last_pos"].data_ptr(), e["max_z"].data_ptr(),
-                                e["n_events"].data_ptr())
+        return _rows_struct(self.el) if self.el is not None else None
 
     def ring_struct(self):
         if self.ring is None:
@@ -271,13 +283,7 @@ def collect(bufs):
     """Copy the results of the last launch back to the host (synchronises)."""
     tally = tally_from_bytes(bufs.tally.cpu().numpy())
     status = int(bufs.status.item())
-    electrons = None
-    if bufs.el is not None:
-        n = bufs.num_el
-        e = {k: v.cpu().numpy() for k, v in bufs.el.items()}
-        electrons = dict(outcome=e["outcome"], flags=e["flags"], final_E=e["final_E"],
-                         dir=e["dir"].reshape(3, n).T.copy(), last_pos=e["last_pos"].reshape(3, n).T.copy(),
-                         max_z=e["max_z"], n_events=e["n_events"])
+    electrons = _host_rows(bufs.el, bufs.num_el) if bufs.el is not None else None
     events, total = None, 0
     if bufs.ring is not None:
         total = int(bufs.cursor.item())
@@ -320,11 +326,12 @@ class Batch:
     """Many simulations run by one persistent kernel.
 
     sims: list of input_par dicts (each with num_el).  Tables are built once
-    per distinct (material, E0, Emin, Wc, tol) and shared.
+    per distinct (material, E0, Emin, Wc, tol) and shared.  electrons=True
+    keeps every simulation's per-electron rows (electrons(k)).
     """
 
     def __init__(self, sims, seed=0, device="cuda", hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T,
-                 quirks=_lib.QUIRKS_REFERENCE, tally_channels=False, first_electron=0):
+                 quirks=_lib.QUIRKS_REFERENCE, tally_channels=False, first_electron=0, electrons=False):
         torch = _torch()
         self.device = torch.device(device)
         self.inputs = [with_defaults(s) for s in sims]
@@ -354,6 +361,12 @@ class Batch:
             self.structs.append(make_sim(p, p["num_el"], seed, first_electron, _lib.FP32, k, hist_E, hist_T, quirks,
                                          _lib.TALLY_CHANNELS if tally_channels else 0))
         self.tables = tabs
+        self.el, self._el_structs = None, []
+        if electrons:
+            self.el = [_device_rows(int(p["num_el"]), torch.float32, self.device) for p in self.inputs]
+            self._el_structs = [_rows_struct(e) for e in self.el]   # read when the batch is packed
+            for s_, eo in zip(self.structs, self._el_structs):
+                s_.electrons = C.addressof(eo)
         self.mats = (_lib.Material * len(mats))(*mats)
         self._sims_arr = (_lib.Sim * self.n)(*self.structs)
         self._tarr = (_lib.Table * max(1, len(tabs)))(*[t.struct for t in tabs]) if tabs else None
@@ -400,3 +413,9 @@ class Batch:
     def collect(self):
         host = self.tallies.cpu().numpy()
         return [tally_from_bytes(host[k]) for k in range(self.n)], int(self.status.item())
+
+    def electrons(self, k):
+        """Simulation k's per-electron rows on the host (electrons=True)."""
+        if self.el is None:
+            raise RuntimeError("the batch keeps no per-electron rows (electrons=False)")
+        return _host_rows(self.el[k], int(self.inputs[k]["num_el"]))

@@ -82,6 +82,27 @@ def test_plain_with_its_table_equals_batched(variant):
         assert np.array_equal(res[k]["hist_E"], ref["hist_E"])
 
 
+def test_batched_rows_equal_plain_rows():
+    """A batch that keeps per-electron rows (mcd_sim.electrons) writes the
+    rows a plain launch writes for the same electrons."""
+    from mcd.tables import ds_tables
+    b = engine.Batch(SIMS, seed=42, electrons=True)
+    b.run(_lib.Tune(256, 0, 1, 0, 0))
+    for k, p in enumerate(SIMS):
+        mat = _lib.material(p["material"])
+        sim = engine.make_sim(p, p["num_el"], seed=42, sim_id=k)
+        engine.use_sigma_table(sim, mat)
+        tabs = None
+        if engine.mode_of(p) == _lib.MODE_DS:
+            tabs = ds_tables(mat, p["E0"], p["Emin"], p["Wc"], p["tol_E"], p["tol_W"])
+        bufs = engine.RunBuffers(p["num_el"], _lib.FP32, True, 0)
+        bufs.zero()
+        engine.launch(sim, mat, tabs, bufs)
+        ref, got = engine.collect(bufs).electrons, b.electrons(k)
+        for key in ("outcome", "flags", "n_events", "final_E", "dir", "last_pos", "max_z"):
+            assert np.array_equal(got[key], ref[key], equal_nan=True), (k, key)
+
+
 @pytest.mark.parametrize("variant", [0, 1])
 def test_tabulated_cross_sections_follow_inline(variant):
     sims = [dict(p, num_el=4 * p["num_el"]) for p in SIMS]

@@ -39,7 +39,7 @@ def test_struct_layouts_match():
 
 def test_abi_and_errors():
     L = _lib.lib()
-    assert L.mcd_abi_version() == _lib.ABI_VERSION == 8
+    assert L.mcd_abi_version() == _lib.ABI_VERSION == 9
     assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
     m = _lib.Material()
     assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
