@@ -407,7 +407,32 @@ def cont_bench(args, dev):
     return {"workload": CONT_WORKLOAD, "num_el": n, "events": ev, "ms": ms_b, "events_per_s": ev / ms_b * 1e3,
             "electrons_per_s": n / ms_b * 1e3, "plain_ms": ms_p, "plain_events_per_s": int(tp["events"]) / ms_p * 1e3,
             "eta": t["bks"] / n, "mean_exit_E_eV": float((hE * mids).sum() / max(1.0, hE.sum())),
+            "cpu_baseline": None if args.no_cpu else oracle_eta_check(
+                args, t["bks"] / n, n, _oracle_material("Cu"), 20000.0, 1000.0, 70.0, min(n, 20000),
+                mode="cont", bethe="JL", max_scatt=10 ** 6),
             "gpu_launches": 2 * args.steps}
+
+
+def _oracle_material(sp):
+    import mcd_oracle as O
+    return O.Material(sp)
+
+
+def oracle_eta_check(args, eta_gpu, n_gpu, om, E0, Emin, tilt, n, **kw):
+    """CPU baseline of a section: the FP64 C oracle on all host threads over
+    the first n electrons of the same workload (same Philox electron indices),
+    its events/s, and the section's backscatter yield against the oracle's
+    (z of the difference; FP32 and FP64 trajectories diverge, so the
+    comparison is statistical)."""
+    import coracle
+    t0 = time.perf_counter()
+    c = coracle.run(om, E0, Emin, tilt, n, seed=args.seed, **kw)
+    dt = time.perf_counter() - t0
+    eta_o = float(np.mean(c["outcome"] == 1))
+    var = eta_gpu * (1 - eta_gpu) / n_gpu + eta_o * (1 - eta_o) / n
+    return {"kind": "port", "cores": os.cpu_count() or 1, "electrons": n,
+            "events_per_s": float(c["n_events"].sum()) / dt, "eta_oracle": eta_o,
+            "z": abs(eta_gpu - eta_o) / max(math.sqrt(var), 1e-12)}
 
 
 DET_WORKLOAD = ("projection of 2^27 float32 exit directions (three planes, 1.61 GB) onto the EBSD detector "
@@ -439,10 +464,23 @@ def detector_bench(args, dev):
     t = statistics.median(times)
     peak = float(measured_peaks().get("hbm_gbs", 6800.0))
     gbs = 20.0 * n / t / 1e9
+    cpu = None
+    if not args.no_cpu:
+        # CPU baseline: the FP64 restatement of projOnDetector (one core, numpy)
+        # on the first 2^20 directions, and the FP32 kernel's error against it
+        import mcd_oracle as O
+        k = 1 << 20
+        v = dirs[:, :k].double().T.cpu().numpy()
+        t0 = time.perf_counter()
+        ref = O.proj_on_detector(v, detector.ALPHA, detector.XY_PC, detector.L)
+        dt = time.perf_counter() - t0
+        err = np.abs(out[:, :k].double().T.cpu().numpy() - ref)
+        cpu = {"kind": "port", "cores": 1, "directions": k, "directions_per_s": k / dt,
+               "max_abs_err_um": float(err.max()), "max_rel_err": float((err / np.maximum(np.abs(ref), 1.0)).max())}
     return {"workload": DET_WORKLOAD, "n": n, "ms": t * 1e3, "directions_per_s": n / t,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "bytes_per_direction": 20, "peak_note": "measured copy bandwidth"},
-            "gpu_launches": max(3, args.steps)}
+            "cpu_baseline": cpu, "gpu_launches": max(3, args.steps)}
 
 
 STREAM_WORKLOAD = ("DS Au, E0 30 keV, Emin 0.5 keV, tilt 70 deg, Wc 50 eV, tol 1e-4, every event streamed "
@@ -470,10 +508,19 @@ def stream_bench(args, dev):
     seen[0] = 0
     torch.cuda.synchronize(dev)
     st = es.run(consumer)
+    eta = sum(t["bks"] for t in st["tallies"]) / n
+    cpu = None
+    if not args.no_cpu:
+        import coracle
+        from mcd import tables
+        dt = tables.ds_tables(_lib.material("Au"), 30000.0, 500.0, 50.0, 1e-4, 1e-4, dev)
+        ht = [coracle.HostTable(t.Ws.cpu().numpy(), t.Es.cpu().numpy(), t.cdf.cpu().numpy()) for t in dt]
+        cpu = oracle_eta_check(args, eta, n, _oracle_material("Au"), 30000.0, 500.0, 70.0, min(n, 2000),
+                               mode="DS", Wc=50.0, tables=ht, max_scatt=10 ** 6)
     return {"workload": STREAM_WORKLOAD, "num_el": n, "chunk": chunk, "events": st["events"],
             "records_received": seen[0], "wall_s": st["wall_s"], "events_per_s": st["events"] / st["wall_s"],
             "drain_GB_per_s": st["bytes"] / st["wall_s"] / 1e9, "record_bytes": es.rec_bytes,
-            "ring_GB": es.cap * es.rec_bytes / 1e9,
+            "ring_GB": es.cap * es.rec_bytes / 1e9, "eta": eta, "cpu_baseline": cpu,
             "reruns": st["reruns"], "gpu_launches": len(es.batches)}
 
 
