@@ -18,12 +18,14 @@
 
 namespace mcd {
 
+// Per-block sums; the per-event counters (events, channels) are 64-bit, as
+// one persistent block can see more than 2^32 events of a channel.
 struct BlockTally {
     unsigned int outcome[8];
     unsigned int double_rows, nan_events, clamped, long_path, table_range, pad_;
     unsigned long long events;
     double sum_E, sum_E2, sum_steps2;
-    unsigned int channel[MCD_MAX_CHANNELS];
+    unsigned long long channel[MCD_MAX_CHANNELS];
 };
 
 __device__ __forceinline__ void bt_zero(BlockTally* t, int n) {
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* 
                                                  : cont_event<T, REC>(L, c, elec, &ev);
             if (ch >= 0) {
                 if (REC) st |= ring_append(ring, (uint32_t)i, L.step, ev);
-                if (chan) atomicAdd(&bt.channel[ch], 1u);
+                if (chan) atomicAdd(&bt.channel[ch], 1ull);
             }
         }
         st |= finish_electron(c, L, i, bt, tally, eo);
@@ -336,7 +338,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
             else
                 ch = cont_event<float, REC>(L, c, c.first + local, &ev);
             if (REC && ch >= 0) st |= ring_append(ring, (uint32_t)local, L.step, ev);
-            if (ch >= 0 && (c.bits & kBitChan)) atomicAdd(&s_t[sim].channel[ch], 1u);
+            if (ch >= 0 && (c.bits & kBitChan)) atomicAdd(&s_t[sim].channel[ch], 1ull);
             if (L.outcome != MCD_OUT_NONE) {
                 const mcd_electron_out& r = rows[sim];
                 const ElOut eo{r.outcome, r.flags, r.final_E, r.dir, r.last_pos, r.max_z, r.n_events};
