@@ -21,7 +21,10 @@ The pool of CPU workers (MapScatterer, MC/doScatter.py:22-95) has no
 counterpart: each chunk is one kernel launch.
 """
 import argparse
+import json
+import math
 import os
+import time
 
 import numpy as np
 
@@ -168,8 +171,10 @@ def _hdf_available():
         return False
 
 
-def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_electron=1000):
-    """Transport inputPar['num_el'] electrons and write the tables.
+def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_electron=1000, block_size=0):
+    """Transport inputPar['num_el'] electrons and write the tables, and a JSON
+    run record beside them (parameters, seed, outcome and channel counts,
+    eta and its standard error, events/s, the OR of the status words).
     fmt: 'h5', 'npz' or None (h5 when pandas and PyTables are present).
     Returns the file name."""
     p = with_defaults(inputPar)
@@ -195,27 +200,65 @@ def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_e
     total = int(p["num_el"])
     epe = float(events_per_electron)
     first = 0
+    record = {"outcomes": {k: 0 for k in _lib.OUTCOME_NAMES}, "channels": {}, "events": 0, "double_rows": 0,
+              "nan_events": 0, "status": 0, "gpu_s": 0.0, "launches": 0}
+    t_start = time.perf_counter()
     while first < total:
         n = min(int(chunk), total - first)
-        sim = make_sim(p, n, seed, first)
+        sim = make_sim(p, n, seed, first, tally_flags=_lib.TALLY_CHANNELS)
         use_sigma_table(sim, mat)
         cap = int(1.3 * epe * n) + 4096 if sc_cols else 0
         while True:
             bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=ring_fields(sc_cols))
             bufs.zero()
-            launch(sim, mat, tables, bufs)
+            t0 = time.perf_counter()
+            launch(sim, mat, tables, bufs, block_size)
             res = collect(bufs)
+            record["gpu_s"] += time.perf_counter() - t0
+            record["launches"] += 1
             if not sc_cols or res.events_total <= cap:
                 break
             cap = int(1.2 * res.events_total) + 4096     # same counters: the re-run is exact
         if sc_cols:
             epe = max(epe, res.events_total / n)
+        _add_to_record(record, res, labels)
         els, scats = chunk_tables(res, n, el_cols, sc_cols, labels)
         writer.append("els", els)
         writer.append("scats", scats)
         first += n
     writer.close()
+    _write_record(name, p, seed, total, record, time.perf_counter() - t_start)
     return name
+
+
+def _add_to_record(record, res, labels):
+    t = res.tally
+    for k in _lib.OUTCOME_NAMES:
+        record["outcomes"][k] += int(t[k])
+    for code, count in enumerate(t["channel"]):
+        if count:
+            lab = str(labels[code]) if code < len(labels) and labels[code] else str(code)
+            record["channels"][lab] = record["channels"].get(lab, 0) + int(count)
+    for k in ("events", "double_rows", "nan_events"):
+        record[k] += int(t[k])
+    record["status"] |= int(res.status)
+
+
+def _device_name():
+    import torch
+    return torch.cuda.get_device_name(torch.cuda.current_device())
+
+
+def _write_record(name, p, seed, n, record, wall_s):
+    """The run record: <store name>.json."""
+    bks = record["outcomes"]["bks"]
+    eta = bks / n if n else float("nan")
+    rec = {"file": os.path.basename(name), "input": {k: str(v) for k, v in p.items()}, "seed": int(seed),
+           "num_el": n, **record, "eta": eta, "eta_sigma": math.sqrt(eta * (1.0 - eta) / n) if n else float("nan"),
+           "events_per_s": record["events"] / record["gpu_s"] if record["gpu_s"] > 0 else None,
+           "wall_s": wall_s, "device": _device_name()}
+    with open(os.path.splitext(name)[0] + ".json", "w") as f:
+        json.dump(rec, f, indent=1)
 
 
 def main(argv=None):
@@ -226,6 +269,8 @@ def main(argv=None):
     ap.add_argument("--format", choices=("h5", "npz"), default=None)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=100_000, help="electrons per kernel launch")
+    ap.add_argument("--block-size", type=int, default=0,
+                    help="threads per block (8, 16 or a multiple of 32 up to 256; 0 = automatic)")
     a = ap.parse_args(argv)
     p = readInput(a.ifile)
     print(" - Number of incident electrons: %s" % p["num_el"])
@@ -233,6 +278,6 @@ def main(argv=None):
     print(" - Scattering mode is: %s" % p["mode"])
     print(" - Elastic scattering mode is: %s" % p.get("elastic", "Ruth_vanilla"))
     out = a.out if a.out.endswith("/") else a.out + "/"
-    name = run(p, out, a.format, a.chunk, a.seed)
+    name = run(p, out, a.format, a.chunk, a.seed, block_size=a.block_size)
     print(" BSE data had been written to ", name)
     return name

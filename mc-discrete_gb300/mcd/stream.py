@@ -83,7 +83,17 @@ class EventStream:
     def run(self, consumer=None):
         """Transport every chunk; consumer(records, chunk_index) gets each host
         piece as a numpy structured array (a view valid during the call).
-        Returns a dict with the event and byte counts and the wall time."""
+        Returns a dict with the event and byte counts and the wall time.  An
+        exception raised by the consumer ends the run: the launches and copies
+        in flight finish first, and the stream can be run again."""
+        torch = _torch()
+        try:
+            return self._run(consumer)
+        except BaseException:
+            torch.cuda.synchronize(self.device)
+            raise
+
+    def _run(self, consumer):
         torch = _torch()
         cs = torch.cuda.current_stream(self.device)
         done = [torch.cuda.Event() for _ in range(2)]

@@ -1,13 +1,14 @@
 """The whole-simulation driver on the GPU: `python -m mcd -i input.file`
 writes the reference's input / els / scats tables (here as .npz; HDF5 where
-pandas and PyTables exist), consistent with the run's own tallies."""
+pandas and PyTables exist), consistent with the run's own tallies, and a
+JSON run record beside them."""
 import subprocess
 import sys
 
 import numpy as np
 import pytest
 
-from mcd import config, doScatter, engine
+from mcd import _lib, config, doScatter, engine
 
 pytestmark = pytest.mark.gpu
 
@@ -51,3 +52,12 @@ def test_cli_writes_reference_tables(tmp_path):
     assert np.allclose(z["scats/energy"], z["scats/E"] - z["scats/E_loss"])
     for c in ("dx", "dy", "dz", "last_x", "last_y", "last_z", "final_E"):
         assert z["els/" + c].size == oc.size
+    # the run record beside the tables
+    import json
+    rec = json.load(open(name[:-4] + ".json"))
+    assert rec["num_el"] == 3000 and rec["seed"] == 0 and rec["launches"] == 3
+    assert rec["outcomes"]["bks"] == t["bks"] and rec["events"] == t["events"]
+    assert sum(rec["channels"].values()) == t["events"]
+    assert set(rec["channels"]) <= {"Ruth", "Moller", "Quinn", "Gryz1s", "Gryz2s", "Gryz2p"}
+    assert abs(rec["eta"] - t["bks"] / 3000) < 1e-12 and rec["events_per_s"] > 0
+    assert rec["status"] & ~_lib.FLAG_NAN == 0          # the reference's NaN angles may be flagged

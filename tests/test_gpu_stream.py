@@ -126,3 +126,24 @@ def test_packed_header_single_ring_equals_full_records(single):
     assert rec.size == ref.size
     for f in ("electron", "step_chan", "E", "W", "pathl", "c2", "half_phi", "x", "y", "z"):
         assert np.array_equal(rec[f], ref[f]), f
+
+
+def test_consumer_exception_ends_the_run_and_the_stream_recovers(single):
+    """A consumer that raises ends the run with its exception, after the work
+    in flight has finished; the same stream then runs to completion."""
+    ref, _ = single
+    es = EventStream(P, chunk=4000, seed=21, events_per_electron=450.0, tune=INLINE, piece_bytes=1 << 22)
+
+    class Stop(Exception):
+        pass
+
+    def bad(rec, c):
+        if c == 1:
+            raise Stop()
+
+    with pytest.raises(Stop):
+        es.run(bad)
+    rec, stats = collect_stream(es)
+    assert stats["events"] == stats["events_tallied"] == rec.size == ref.size
+    rec = key(rec)
+    assert np.array_equal(rec["W"], ref["W"]) and np.array_equal(rec["electron"], ref["electron"])
