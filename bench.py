@@ -369,7 +369,8 @@ def cont_bench(args, dev):
     n = max(1000, int(round(1e6 * args.scale)))
     p = dict(material="Cu", E0=20000.0, Emin=1000.0, s_tilt=70.0, mode="cont", Bethe_model="JL", num_el=n)
     b = engine.Batch([p], seed=args.seed, device=dev)
-    tune = _lib.Tune(1024, 0, 1, 0, 0)
+    from mcd import autotune
+    tune, _ = autotune.tune(b)
     sim = engine.make_sim(p, n, seed=args.seed)
     mat = _lib.material("Cu")
     bufs = engine.RunBuffers(n, _lib.FP32, False, 0, device=dev)
@@ -407,6 +408,7 @@ def cont_bench(args, dev):
     return {"workload": CONT_WORKLOAD, "num_el": n, "events": ev, "ms": ms_b, "events_per_s": ev / ms_b * 1e3,
             "electrons_per_s": n / ms_b * 1e3, "plain_ms": ms_p, "plain_events_per_s": int(tp["events"]) / ms_p * 1e3,
             "eta": t["bks"] / n, "mean_exit_E_eV": float((hE * mids).sum() / max(1.0, hE.sum())),
+            "tune": {"block": tune.block_size, "refill": tune.refill, "variant": tune.variant},
             "cpu_baseline": None if args.no_cpu else oracle_eta_check(
                 args, t["bks"] / n, n, _oracle_material("Cu"), 20000.0, 1000.0, 70.0, min(n, 20000),
                 mode="cont", bethe="JL", max_scatt=10 ** 6),
