@@ -18,7 +18,9 @@ shell labels such as 'Gryz3s3p3d'); otherwise to a NumPy .npz file with
 keys 'input/<name>', 'els/<column>' and 'scats/<column>'.
 
 The pool of CPU workers (MapScatterer, MC/doScatter.py:22-95) has no
-counterpart: each chunk is one kernel launch.
+counterpart: each chunk is one kernel launch, on the persistent batched
+kernel unless scatter_output is asked for (then a plain launch fills an
+event ring) or a block size is given.
 """
 import argparse
 import json
@@ -30,7 +32,7 @@ import numpy as np
 
 from . import _lib
 from .config import readInput, with_defaults
-from .engine import collect, launch, make_sim, mode_of, RunBuffers, use_sigma_table
+from .engine import Batch, collect, launch, make_sim, mode_of, RunBuffers, RunResult, use_sigma_table
 from .tables import ds_tables
 
 EL_COLS = ("outcome", "final_E", "final_dir", "last_pos")
@@ -205,22 +207,12 @@ def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_e
     t_start = time.perf_counter()
     while first < total:
         n = min(int(chunk), total - first)
-        sim = make_sim(p, n, seed, first, tally_flags=_lib.TALLY_CHANNELS)
-        use_sigma_table(sim, mat)
-        cap = int(1.3 * epe * n) + 4096 if sc_cols else 0
-        while True:
-            bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=ring_fields(sc_cols))
-            bufs.zero()
-            t0 = time.perf_counter()
-            launch(sim, mat, tables, bufs, block_size)
-            res = collect(bufs)
-            record["gpu_s"] += time.perf_counter() - t0
-            record["launches"] += 1
-            if not sc_cols or res.events_total <= cap:
-                break
-            cap = int(1.2 * res.events_total) + 4096     # same counters: the re-run is exact
-        if sc_cols:
-            epe = max(epe, res.events_total / n)
+        if sc_cols or block_size:
+            res = _plain_chunk(p, n, seed, first, mat, tables, block_size, sc_cols, epe, record)
+            if sc_cols:
+                epe = max(epe, res.events_total / n)
+        else:
+            res = _batched_chunk(p, n, seed, first, record)
         _add_to_record(record, res, labels)
         els, scats = chunk_tables(res, n, el_cols, sc_cols, labels)
         writer.append("els", els)
@@ -229,6 +221,39 @@ def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_e
     writer.close()
     _write_record(name, p, seed, total, record, time.perf_counter() - t_start)
     return name
+
+
+def _plain_chunk(p, n, seed, first, mat, tables, block_size, sc_cols, epe, record):
+    """One chunk as one plain launch, with its events in a device ring."""
+    sim = make_sim(p, n, seed, first, tally_flags=_lib.TALLY_CHANNELS)
+    use_sigma_table(sim, mat)
+    cap = int(1.3 * epe * n) + 4096 if sc_cols else 0
+    while True:
+        bufs = RunBuffers(n, _lib.FP32, True, cap, ring_fields=ring_fields(sc_cols))
+        bufs.zero()
+        t0 = time.perf_counter()
+        launch(sim, mat, tables, bufs, block_size)
+        res = collect(bufs)
+        record["gpu_s"] += time.perf_counter() - t0
+        record["launches"] += 1
+        if not sc_cols or res.events_total <= cap:
+            return res
+        cap = int(1.2 * res.events_total) + 4096     # same counters: the re-run is exact
+
+
+def _batched_chunk(p, n, seed, first, record):
+    """One chunk on the persistent kernel (a warp refills its lanes from the
+    queue as electrons finish), keeping the per-electron rows; the same
+    electrons and cross-section table as the plain launch, so the same rows."""
+    from .autotune import tune
+    b = Batch([dict(p, num_el=n)], seed=seed, first_electron=first, electrons=True, tally_channels=True)
+    t_ = tune(b)[0]
+    t0 = time.perf_counter()
+    tallies, status = b.run(t_)
+    rows = b.electrons(0)
+    record["gpu_s"] += time.perf_counter() - t0
+    record["launches"] += 1
+    return RunResult(tallies[0], status, rows, None, 0)
 
 
 def _add_to_record(record, res, labels):

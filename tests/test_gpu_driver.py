@@ -61,3 +61,20 @@ def test_cli_writes_reference_tables(tmp_path):
     assert set(rec["channels"]) <= {"Ruth", "Moller", "Quinn", "Gryz1s", "Gryz2s", "Gryz2p"}
     assert abs(rec["eta"] - t["bks"] / 3000) < 1e-12 and rec["events_per_s"] > 0
     assert rec["status"] & ~_lib.FLAG_NAN == 0          # the reference's NaN angles may be flagged
+
+
+def test_rows_only_run_uses_the_batched_kernel_with_the_same_rows(tmp_path, monkeypatch):
+    """Without scatter_output the driver runs each chunk on the persistent
+    kernel; its rows equal those of plain launches of the same electrons."""
+    monkeypatch.setenv("MCD_CACHE_DIR", str(tmp_path / "cache"))
+    p = config.parse_input(INPUT.replace("scatter_output : type, E, E_loss, pol_angle, az_angle, pathl, position, energy",
+                                         "scatter_output :"))
+    assert not [c for c in p.get("scatter_output", []) if c]
+    name = doScatter.run(p, str(tmp_path) + "/", "npz", chunk=1000, seed=0)
+    z = np.load(name)
+    g = engine.run(p, num_el=3000, seed=0, tabulated=True)
+    e = g.electrons
+    reps = 1 + (e["flags"] & 1).astype(np.int64)
+    assert np.array_equal(z["els/final_E"], np.repeat(e["final_E"].astype(np.float64), reps))
+    assert np.array_equal(z["els/dz"], np.repeat(e["dir"][:, 2].astype(np.float64), reps))
+    assert "scats/type" not in z.files
