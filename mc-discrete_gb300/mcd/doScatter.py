@@ -18,9 +18,9 @@ shell labels such as 'Gryz3s3p3d'); otherwise to a NumPy .npz file with
 keys 'input/<name>', 'els/<column>' and 'scats/<column>'.
 
 The pool of CPU workers (MapScatterer, MC/doScatter.py:22-95) has no
-counterpart: each chunk is one kernel launch, on the persistent batched
-kernel unless scatter_output is asked for (then a plain launch fills an
-event ring) or a block size is given.
+counterpart: each chunk is one launch of the persistent batched kernel
+(with an event ring when scatter_output is asked for), or a plain launch
+when a block size is given.
 """
 import argparse
 import json
@@ -207,12 +207,12 @@ def run(inputPar, path="../data/", fmt=None, chunk=100_000, seed=0, events_per_e
     t_start = time.perf_counter()
     while first < total:
         n = min(int(chunk), total - first)
-        if sc_cols or block_size:
+        if block_size:
             res = _plain_chunk(p, n, seed, first, mat, tables, block_size, sc_cols, epe, record)
-            if sc_cols:
-                epe = max(epe, res.events_total / n)
         else:
-            res = _batched_chunk(p, n, seed, first, record)
+            res = _batched_chunk(p, n, seed, first, sc_cols, epe, record)
+        if sc_cols:
+            epe = max(epe, res.events_total / n)
         _add_to_record(record, res, labels)
         els, scats = chunk_tables(res, n, el_cols, sc_cols, labels)
         writer.append("els", els)
@@ -241,19 +241,27 @@ def _plain_chunk(p, n, seed, first, mat, tables, block_size, sc_cols, epe, recor
         cap = int(1.2 * res.events_total) + 4096     # same counters: the re-run is exact
 
 
-def _batched_chunk(p, n, seed, first, record):
+def _batched_chunk(p, n, seed, first, sc_cols, epe, record):
     """One chunk on the persistent kernel (a warp refills its lanes from the
-    queue as electrons finish), keeping the per-electron rows; the same
-    electrons and cross-section table as the plain launch, so the same rows."""
+    queue as electrons finish), keeping the per-electron rows and, for
+    scatter_output, every event in a device ring; the same electrons and
+    cross-section table as a plain launch, so the same rows and events."""
     from .autotune import tune
     b = Batch([dict(p, num_el=n)], seed=seed, first_electron=first, electrons=True, tally_channels=True)
     t_ = tune(b)[0]
-    t0 = time.perf_counter()
-    tallies, status = b.run(t_)
-    rows = b.electrons(0)
-    record["gpu_s"] += time.perf_counter() - t0
-    record["launches"] += 1
-    return RunResult(tallies[0], status, rows, None, 0)
+    cap = int(1.3 * epe * n) + 4096
+    while True:
+        t0 = time.perf_counter()
+        if sc_cols:
+            tallies, status, events, total = b.run_events(cap, ring_fields(sc_cols), t_)
+        else:
+            (tallies, status), events, total = b.run(t_), None, 0
+        rows = b.electrons(0)
+        record["gpu_s"] += time.perf_counter() - t0
+        record["launches"] += 1
+        if not sc_cols or total <= cap:
+            return RunResult(tallies[0], status, rows, events, total)
+        cap = int(1.2 * total) + 4096     # same counters: the re-run is exact
 
 
 def _add_to_record(record, res, labels):

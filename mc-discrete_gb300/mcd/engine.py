@@ -405,6 +405,30 @@ class Batch:
         self.tallies.zero_()
         self.status.zero_()
 
+    def run_events(self, capacity, fields=0, tune=None, stream=None):
+        """One run with every event appended to a device ring of `capacity`
+        records (mcd_run_batched_ring; `fields` as for RunBuffers).  Returns
+        (tallies, status, events, events_total): the events on the host in
+        the 8-byte-header form, or None when they outgrew the ring
+        (status has FLAG_RING_FULL; a re-run with a larger ring is exact)."""
+        torch = _torch()
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        rb = event_bytes(fields)
+        ring = torch.empty(int(capacity) * rb, dtype=torch.uint8, device=self.device)
+        cursor = torch.zeros(1, dtype=torch.int64, device=self.device)
+        t = tune if tune is not None else _lib.Tune(256, 0, 1, 0, 0)
+        rs = _lib.EventRing(ring.data_ptr(), int(capacity), cursor.data_ptr(), int(fields), 0)
+        self.zero()
+        code = _lib.lib().mcd_run_batched_ring(self.ws_ptr, self.n, self.tallies.data_ptr(), C.byref(t), C.byref(rs),
+                                               self.status.data_ptr(), st.cuda_stream)
+        _lib.check("mcd_run_batched_ring", code)
+        tallies, status = self.collect()
+        total = int(cursor.item())
+        if total > capacity:
+            return tallies, status | _lib.FLAG_RING_FULL, None, total
+        rec = ring[:total * rb].cpu().numpy().view(event_dtype(fields)).reshape(-1)
+        return tallies, status, unpack_events(rec, fields), total
+
     def run(self, tune=None):
         self.zero()
         self.launch(tune)

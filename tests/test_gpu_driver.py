@@ -40,8 +40,12 @@ def test_cli_writes_reference_tables(tmp_path):
     z = np.load(name)
     assert str(z["input/material"]) == "Si" and str(z["input/num_el"]) == "3000"
     oc = z["els/outcome"]
-    # the same electrons (indices 0..2999, seed 0) with the same cross-section table
-    g = engine.run(p, num_el=3000, seed=0, tabulated=True)
+    # the same electrons (indices 0..2999, seed 0) with the same cross-section
+    # table, as plain launches: the same tallies and the same events
+    g = engine.run(p, num_el=3000, seed=0, tabulated=True, ring_capacity=3000 * 1500)
+    ev = g.events[np.lexsort((g.events["step_chan"] >> 5, g.events["electron"]))]
+    assert np.array_equal(z["scats/E"], ev["E"].astype(np.float64))
+    assert np.array_equal(z["scats/E_loss"], ev["W"].astype(np.float64))
     t = g.tally
     assert (oc == "bks").sum() == t["bks"] and (oc == "abs").sum() == t["abs"] + t["double_rows"]
     assert oc.size == 3000 + t["double_rows"]
