@@ -298,7 +298,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
     const unsigned lt = (1u << lane) - 1u;
     Lane<float> L;
     int sim = 0;
-    uint64_t local = 0;
+    uint64_t elec = 0;
     bool have = false;
     bool exhausted = false;
     uint32_t st = 0;
@@ -318,7 +318,7 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
                         if (s_pre[mid] <= g) lo = mid; else hi = mid;
                     }
                     sim = s_perm[lo];
-                    local = g - s_pre[lo];
+                    elec = s_c[sim].first + (g - s_pre[lo]);   // the Philox electron index
                     lane_init(L, s_c[sim]);
                     have = true;
                 }
@@ -334,15 +334,15 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
             EventOut<float> ev;
             int ch;
             if (!(c.bits & kBitCont))
-                ch = ds_event<float, REC>(L, c, c.first + local, &ev, !inline_sigma && c.sig != nullptr);
+                ch = ds_event<float, REC>(L, c, elec, &ev, !inline_sigma && c.sig != nullptr);
             else
-                ch = cont_event<float, REC>(L, c, c.first + local, &ev);
-            if (REC && ch >= 0) st |= ring_append(ring, (uint32_t)local, L.step, ev);
+                ch = cont_event<float, REC>(L, c, elec, &ev);
+            if (REC && ch >= 0) st |= ring_append(ring, (uint32_t)(elec - c.first), L.step, ev);
             if (ch >= 0 && (c.bits & kBitChan)) atomicAdd(&s_t[sim].channel[ch], 1ull);
             if (L.outcome != MCD_OUT_NONE) {
                 const mcd_electron_out& r = rows[sim];
                 const ElOut eo{r.outcome, r.flags, r.final_E, r.dir, r.last_pos, r.max_z, r.n_events};
-                st |= finish_electron(c, L, local, s_t[sim], tallies + sim, eo);
+                st |= finish_electron(c, L, elec - c.first, s_t[sim], tallies + sim, eo);
                 have = false;
             }
         }
