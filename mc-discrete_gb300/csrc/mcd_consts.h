@@ -111,7 +111,10 @@ struct SimConst {
     uint32_t bits;
 };
 
-constexpr uint32_t kBitDiff = 1u << 3, kBitCont = 1u << 4, kBitChan = 1u << 5, kBitR2 = 1u << 6;
+// kBitFilm: a finite thickness, so that a semi-infinite sample skips the
+// bottom-face test (and its shared-memory load) on every step
+constexpr uint32_t kBitDiff = 1u << 3, kBitCont = 1u << 4, kBitChan = 1u << 5, kBitR2 = 1u << 6,
+                   kBitFilm = 1u << 7;
 template <class C>
 __host__ __device__ __forceinline__ int bits_K(const C& c) { return (int)((c.bits >> 8) & 15u); }
 template <class C>
@@ -233,6 +236,7 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     }
     c.bits = (c.quirks & 7u) | (c.diff ? kBitDiff : 0u) | (c.mode == MCD_MODE_CONT ? kBitCont : 0u) |
              ((c.tally_flags & MCD_TALLY_CHANNELS) ? kBitChan : 0u) | (c.ruth_r2 ? kBitR2 : 0u) |
+             ((s.thickness > 0 && s.thickness < 1e30) ? kBitFilm : 0u) |
              ((uint32_t)c.sig_K << 8) | ((uint32_t)c.sig_S << 12);
     return c;
 }

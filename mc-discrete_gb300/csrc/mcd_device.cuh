@@ -261,7 +261,7 @@ __device__ __forceinline__ void lane_move(Lane<T>& L, const C& c, T s) {
     if (nz <= (T)0) {
         L.outcome = MCD_OUT_BKS;
         L.E_row = L.E;
-    } else if (nz >= c.thickness) {
+    } else if ((c.bits & kBitFilm) && nz >= c.thickness) {
         L.outcome = (L.flags & F_DIFFRACTING) ? MCD_OUT_TRDF : MCD_OUT_TRSM;
         L.E_row = L.E;
     } else {
@@ -348,7 +348,8 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     const float4 x0 = __ldg(reinterpret_cast<const float4*>(r0));
     const float4 y0 = __ldg(reinterpret_cast<const float4*>(r1));
     const float tot = fmaf(f, y0.x - x0.x, x0.x);
-    const float all = fmaf(E, c.dS, tot);   // + diffraction (dS = 0 when off)
+    float all = tot;
+    if (c.bits & kBitDiff) all = fmaf(E, c.dS, tot);   // + diffraction
     *Etot_out = all;
     const float target = U * all;
     if ((c.bits & kBitDiff) && target > tot) return MCD_CH_DIFF;
