@@ -242,6 +242,8 @@ def test_packed_header_records_unpack_in_ring_order():
     assert list(u["step_chan"] >> 5) == [0, 1, 0, 1, 0, 1, 2]
     assert np.array_equal(u["W"], 10.0 * u["electron"] + (u["step_chan"] >> 5))
     assert list(u["step_chan"] & 31) == [0, 1, 3, 2, 1, 2, 0]
+    empty = engine.unpack_events(np.zeros(0, dtype=dt), fields)
+    assert empty.size == 0 and empty.dtype.names == ("electron", "step_chan", "W")
 
 
 def test_c_caller_links_and_runs(tmp_path):
