@@ -395,7 +395,7 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * memory through its own arena; a caller for which an allocation, which can
  * synchronise the device, would break its latency budget).  No counterpart
  * in the reference.  Its scratch is a static device array sized for
- * MCD_STATIC_MAX_SIMS simulations (32 KiB), resident on every GPU that
+ * MCD_STATIC_MAX_SIMS simulations (31.5 KiB), resident on every GPU that
  * loads the library until exit; more simulations return MCD_ETOOBIG.  The
  * first call on a device looks up that array's address (issue it before any
  * stream capture).  Calls share the array: calls that overlap on the GPU

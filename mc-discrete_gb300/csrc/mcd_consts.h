@@ -103,7 +103,7 @@ struct SimConst {
     // E * sigma varies slowly in log E, so linear interpolation at 128 rows
     // per octave is within 3e-7 of the exact sums (relative to the total).
     const float* sig;
-    float sig_l0, sig_inv, sig_tmax;
+    float sig_l0, sig_inv, sig_tmax, sig_off;   // sig_off = -sig_l0 * sig_inv
     int32_t sig_K, sig_S, sig_rows;
     // the small fields the event code tests, packed so that one load serves
     // them all: quirks (bits 0-2, the MCD_Q_* masks), kBit* flags, sig_K
@@ -226,13 +226,14 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     // the caller's table (mcd_run), or none until a batch shares one among
     // the simulations it fits
     c.sig = nullptr;
-    c.sig_l0 = c.sig_inv = c.sig_tmax = 0.0f;
+    c.sig_l0 = c.sig_inv = c.sig_tmax = c.sig_off = 0.0f;
     c.sig_K = m.n_shells + 3;
     c.sig_S = (c.sig_K + 3) & ~3;
     c.sig_rows = 0;
     if (s.sigma_table && s.mode == MCD_MODE_DS) {
         c.sig = s.sigma_table;
         sigma_grid(s.Emin, s.E0, &c.sig_l0, &c.sig_inv, &c.sig_tmax, &c.sig_rows);
+        c.sig_off = -c.sig_l0 * c.sig_inv;
     }
     c.bits = (c.quirks & 7u) | (c.diff ? kBitDiff : 0u) | (c.mode == MCD_MODE_CONT ? kBitCont : 0u) |
              ((c.tally_flags & MCD_TALLY_CHANNELS) ? kBitChan : 0u) | (c.ruth_r2 ? kBitR2 : 0u) |

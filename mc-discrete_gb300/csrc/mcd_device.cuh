@@ -336,7 +336,7 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_ph
 // of E * (running sum); the comparison with U * E * total needs no division.
 template <class C>
 __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Etot_out) {
-    float t = (__log2f(E) - c.sig_l0) * c.sig_inv;
+    float t = fmaf(__log2f(E), c.sig_inv, c.sig_off);
     t = fminf(fmaxf(t, 0.0f), c.sig_tmax);
     const int i = (int)t;
     const float f = t - (float)i;
@@ -372,6 +372,19 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     if (j == 1) return MCD_CH_MOLLER;
     if (j == K - 1) return MCD_CH_QUINN;
     return MCD_CH_GRYZ0 + (j - 2);
+}
+
+// Rutherford sin^2(theta/2) = a U / (a + 1 - U), a = a0 / E
+// (MC/tools/scattering.py:125-152); in FP32 with one division as
+// a0 U / (a0 + E (1 - U)).
+template <class T, class C>
+__device__ __forceinline__ T ruth_s2(const C& c, T E, uint32_t u) {
+    if constexpr (sizeof(T) == 4) {
+        return Ops<T>::div(c.a0 * Ops<T>::unit(u), fmaf(E, Ops<T>::unit_c(u), c.a0));
+    } else {
+        const T a = Ops<T>::div(c.a0, E);
+        return Ops<T>::div(a * Ops<T>::unit(u), a + Ops<T>::unit_c(u));
+    }
 }
 
 // The 'long' check that opens every event (MC/tools/singleScatter.py:19-23).
@@ -447,9 +460,8 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     // --- energy loss and polar angle (MC/tools/scattering.py:568-679)
     T W, s2;
     if (ch == MCD_CH_RUTH) {
-        const T a = Ops<T>::div(c.a0, E);
         W = (T)0;
-        s2 = Ops<T>::div(a * Ops<T>::unit(r.z), a + Ops<T>::unit_c(r.z));
+        s2 = ruth_s2<T>(c, E, r.z);
     } else if (ch == MCD_CH_QUINN) {
         W = c.Epl;
         s2 = (T)0;
@@ -521,8 +533,7 @@ __device__ __forceinline__ int cont_event_r(Lane<T>& L, const C& c, const uint4 
         L.clamp_n += 1;
         dE = E;
     }
-    const T a = Ops<T>::div(c.a0, E);
-    const T s2 = Ops<T>::div(a * Ops<T>::unit(r.z), a + Ops<T>::unit_c(r.z));
+    const T s2 = ruth_s2<T>(c, E, r.z);
     const T uphi = Ops<T>::unit(r.w);
     if (REC) {
         ev->s2 = s2;

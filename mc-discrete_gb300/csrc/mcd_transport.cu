@@ -444,6 +444,7 @@ inline void share_sigma_tables(const mcd_sim* sims, int nsims, const SimConst<do
                 cs[j].sig_inv = inv;
                 cs[j].sig_tmax = tmax;
                 cs[j].sig_rows = rows;
+                cs[j].sig_off = -l0 * inv;
             }
     }
 }
