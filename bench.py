@@ -47,15 +47,15 @@ CPU_SAMPLE_PER_SIM = 600
 # the figure does not grow with the electrons)
 BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
 # warp instructions issued per event by the batched kernel on this workload,
-# from an ncu capture of a quarter-size launch (2.044e10 instructions for
+# from an ncu capture of a quarter-size launch (2.030e10 instructions for
 # 1.3855e9 events); the issue peak is one warp instruction per scheduler
 # per cycle, 4 schedulers per SM
-WARP_INST_PER_EVENT = 14.75
+WARP_INST_PER_EVENT = 14.65
 # the same capture's unit fractions (of peak sustained): issue-active cycles,
 # threads per warp instruction / 32, the L1/TEX unit, its shared-memory
 # wavefronts, and L2
-BATCHED_NCU = {"issue_active": 0.766, "warp_execution_efficiency": 0.712, "l1tex_throughput": 0.707,
-               "shared_wavefronts": 0.283, "l2_throughput": 0.018,
+BATCHED_NCU = {"issue_active": 0.765, "warp_execution_efficiency": 0.711, "l1tex_throughput": 0.711,
+               "shared_wavefronts": 0.284, "l2_throughput": 0.018,
                "capture": "ncu --set full of k_batched on a quarter of the workload (1.3855e9 events)"}
 
 
