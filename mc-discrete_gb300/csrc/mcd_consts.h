@@ -58,7 +58,13 @@ struct TableDev {
 };
 
 template <class T>
-struct SimConst {
+struct __align__(16) SimConst {
+    // the words every event reads first, as one 16-byte load: Philox
+    // counter word 3, the key, and the events before 'long' (at most
+    // 2^32 - 1, the counter word's range)
+    uint32_t sim_id;
+    uint32_t key0, key1;
+    uint32_t max_scatt;
     // transport
     T E0, Emin, thickness;
     T d0x, d0y, d0z;
@@ -86,9 +92,6 @@ struct SimConst {
     int32_t bethe;
     uint32_t quirks;
     uint32_t tally_flags;
-    uint32_t sim_id;
-    uint32_t key0, key1;
-    uint32_t max_scatt;   // events before 'long', at most 2^32 - 1 (the counter word)
     uint64_t first;
     int64_t num_el;
     int32_t hE, hT;

@@ -387,17 +387,6 @@ __device__ __forceinline__ T ruth_s2(const C& c, T E, uint32_t u) {
     }
 }
 
-// The 'long' check that opens every event (MC/tools/singleScatter.py:19-23).
-template <class T, class C>
-__device__ __forceinline__ bool lane_long(Lane<T>& L, const C& c) {
-    if (L.step >= c.max_scatt) {
-        L.outcome = MCD_OUT_LONG;
-        L.E_row = L.E;
-        return true;
-    }
-    return false;
-}
-
 __device__ __forceinline__ uint4 event_counter(uint32_t step, uint64_t elec, uint32_t sim_id) {
     return make_uint4(step, (uint32_t)elec, (uint32_t)(elec >> 32), sim_id);
 }
@@ -501,11 +490,23 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     return ch;
 }
 
+// sim_id, key0, key1, max_scatt in one load: the 'long' check that opens
+// every event (MC/tools/singleScatter.py:19-23) and its Philox block
+template <class C>
+__device__ __forceinline__ uint4 event_words(const C& c) {
+    return *reinterpret_cast<const uint4*>(&c.sim_id);
+}
+
 template <class T, bool REC, class C>
 __device__ __forceinline__ int ds_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev,
                                         bool use_tab = false) {
-    if (lane_long(L, c)) return -1;
-    const uint4 r = philox(event_counter(L.step, elec, c.sim_id), c.key0, c.key1);
+    const uint4 w = event_words(c);
+    if (L.step >= w.w) {
+        L.outcome = MCD_OUT_LONG;
+        L.E_row = L.E;
+        return -1;
+    }
+    const uint4 r = philox(event_counter(L.step, elec, w.x), w.y, w.z);
     L.step += 1;
     return ds_event_r<T, REC>(L, c, r, ev, use_tab);
 }
@@ -560,8 +561,13 @@ __device__ __forceinline__ int cont_event_r(Lane<T>& L, const C& c, const uint4 
 
 template <class T, bool REC, class C>
 __device__ __forceinline__ int cont_event(Lane<T>& L, const C& c, uint64_t elec, EventOut<T>* ev) {
-    if (lane_long(L, c)) return -1;
-    const uint4 r = philox(event_counter(L.step, elec, c.sim_id), c.key0, c.key1);
+    const uint4 w = event_words(c);
+    if (L.step >= w.w) {
+        L.outcome = MCD_OUT_LONG;
+        L.E_row = L.E;
+        return -1;
+    }
+    const uint4 r = philox(event_counter(L.step, elec, w.x), w.y, w.z);
     L.step += 1;
     return cont_event_r<T, REC>(L, c, r, ev);
 }
