@@ -11,8 +11,6 @@ The default geometry is the reference's (MC/tools/parameters.py:22-33):
 L = 15250 um, sample tilt 70 deg, theta_C = 0, alpha = 90 - 70 + 0 deg,
 pixel pitch 49.375 um, pattern centre (3.57, 113.45) pixels.
 """
-import ctypes as C
-
 import numpy as np
 
 from . import _lib

@@ -18,8 +18,6 @@ stream makes the re-run exact.
 import ctypes as C
 import time
 
-import numpy as np
-
 from . import _lib
 from .config import with_defaults
 from .engine import Batch, _torch, event_dtype

@@ -33,7 +33,6 @@ Deliberate choices, each forced by running the reference here:
     MC/tools/multiScatter.py:206-207 vs MC/tools/singleScatter.py:205); the
     replay part runs the loop of trajectory_cont_cl with maxz passed.
 """
-import math
 import multiprocessing as mp
 import os
 import random

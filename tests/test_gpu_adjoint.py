@@ -12,7 +12,6 @@ import numpy as np
 import pytest
 import torch
 
-from mcd import _lib
 from mcd.adjoint import ExitEnergyModel, exit_histogram
 from _gpu_util import input_par
 

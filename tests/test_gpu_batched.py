@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from mcd import _lib, engine
-from _gpu_util import eta_z, input_par
+from _gpu_util import input_par
 
 pytestmark = pytest.mark.gpu
 
