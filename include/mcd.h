@@ -398,11 +398,16 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * MCD_STATIC_MAX_SIMS simulations (31.5 KiB), resident on every GPU that
  * loads the library until exit; more simulations return MCD_ETOOBIG.  The
  * first call on a device looks up that array's address (issue it before any
- * stream capture).  Calls share the array: calls that overlap on the GPU
- * race.  The simulations are packed on the host and copied in on `stream`;
+ * stream capture) and keeps it for the life of the device's primary
+ * context: do not use the library across a cudaDeviceReset.  Calls share
+ * the array: calls that overlap on the GPU race.  The simulations are
+ * packed on the host and handed to a staging kernel on `stream` as one
+ * kernel argument, so no host memory has to outlive the call;
  * tallies[nsims] (zeroed by the caller) and status are device pointers.
- * Cross sections are evaluated inline unless a simulation carries a
- * caller-built sigma_table.                                                 */
+ * tune is read as by mcd_run_batched (variant bit 0: the 48-register
+ * kernel; bit 1: inline cross sections).  Without bit 1 a simulation that
+ * carries a caller-built sigma_table reads it; the others evaluate their
+ * cross sections inline (there is no room for tables in the array).       */
 #define MCD_STATIC_MAX_SIMS 64
 int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims,
                             const mcd_material* mats, const int32_t* sim_material,

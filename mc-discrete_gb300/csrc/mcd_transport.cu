@@ -698,6 +698,12 @@ extern "C" int mcd_run_batched_ring(void* workspace, int32_t nsims, mcd_tally* t
 // in full (the queue counter starts at zero each call), so calls that overlap
 // on the GPU - two streams, or two host threads - race on it and must not be
 // issued concurrently.
+//
+// The host packs the scratch and hands it to a staging kernel as one
+// by-value argument (kernel arguments may take up to 32764 bytes), which
+// writes it into the array ahead of the transport launch on the same
+// stream: no host buffer has to outlive the call, and nothing is copied
+// from pageable memory.
 // ---------------------------------------------------------------------------
 #include <mutex>
 
@@ -706,8 +712,20 @@ namespace mcd {
 constexpr int kStaticMaxSims = MCD_STATIC_MAX_SIMS;
 constexpr size_t kStaticHeadBytes = batch_consts_off(kStaticMaxSims);
 constexpr size_t kStaticScratchBytes = batch_core_bytes(kStaticMaxSims);
+static_assert(kStaticScratchBytes % 16 == 0, "the scratch is staged as 16-byte words");
+
+struct StaticBlock {
+    uint4 w[kStaticScratchBytes / 16];
+};
+static_assert(sizeof(StaticBlock) + 16 <= 32764, "the packed scratch must fit the kernel argument space");
 
 static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
+
+// Writes the first `words` 16-byte words of the packed block to dst.
+__global__ void __launch_bounds__(256) k_static_stage(uint4* dst, const StaticBlock blk, uint32_t words) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x)
+        dst[i] = blk.w[i];
+}
 
 constexpr int kStaticMaxDevices = 64;
 static std::mutex g_static_mu;
@@ -715,6 +733,8 @@ static void* g_static_ptr[kStaticMaxDevices];
 
 // The device address of g_static_scratch on the current device, looked up
 // once per device (host code may not use the symbol itself as an address).
+// The address belongs to the device's primary context: a cudaDeviceReset
+// makes it stale, so the library must not be used across one.
 static int static_scratch(void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
@@ -746,9 +766,15 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     }
     if (block % 32 != 0 || block > 1024 || refill < 1 || refill > 32 || (tune && tune->reserved != 0))
         return MCD_EINVAL;
+    // the variant bits of mcd_run_batched: bit 0 the 48-register kernel,
+    // bit 1 inline cross sections (a caller-built sigma_table is then not read)
+    const bool lowreg = tune && (tune->variant & 1);
+    const int inline_sigma = (tune && (tune->variant & 2)) ? 1 : 0;
+    if (lowreg && block > 256) return MCD_EINVAL;
 
-    // pack on the host stack: header (queue = 0), prefix sums, constants
-    alignas(256) uint8_t host[kStaticScratchBytes];
+    // pack on the host: header (queue = 0), prefix sums, constants, row pointers
+    StaticBlock blk;
+    uint8_t* host = reinterpret_cast<uint8_t*>(&blk);
     memset(host, 0, kStaticHeadBytes);
     BatchHeader* h = reinterpret_cast<BatchHeader*>(host);
     unsigned long long* pre = reinterpret_cast<unsigned long long*>(host + batch_prefix_off());
@@ -782,7 +808,7 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     pack_rows(sims, nsims, host);
     // the core only: cross sections come from the callers' tables or are
     // evaluated inline
-    const size_t bytes = batch_core_bytes(nsims);
+    const uint32_t words = (uint32_t)((batch_core_bytes(nsims) + 15) / 16);
 
     void* scratch = nullptr;
     int rc = static_scratch(&scratch);
@@ -791,18 +817,18 @@ extern "C" int mcd_run_batched_noalloc(const mcd_sim* sims, int32_t nsims, const
     if (cudaGetDevice(&dev) != cudaSuccess) return MCD_ECUDA;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCD_ECUDA;
     const size_t smem = batch_smem(nsims);
+    auto kern = lowreg ? k_batched_lr<false> : k_batched<false>;
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(k_batched<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return MCD_ECUDA;
     int fit = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_batched<false>, block, smem) != cudaSuccess)
-        return MCD_ECUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kern, block, smem) != cudaSuccess) return MCD_ECUDA;
     if (fit < 1) return MCD_ETOOBIG;
     if (per_sm <= 0 || per_sm > fit) per_sm = fit;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // pageable source: the call returns once `host` has been staged, so the
-    // stack buffer may go out of scope afterwards
-    if (cudaMemcpyAsync(scratch, host, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) return MCD_ECUDA;
-    k_batched<false><<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(scratch), tallies, refill, status);
+    k_static_stage<<<(words + 255) / 256, 256, 0, st>>>(static_cast<uint4*>(scratch), blk, words);
+    if (cudaGetLastError() != cudaSuccess) return MCD_ECUDA;
+    kern<<<sms * per_sm, block, smem, st>>>(static_cast<uint8_t*>(scratch), tallies, refill, status,
+                                            mcd_event_ring{}, inline_sigma);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }

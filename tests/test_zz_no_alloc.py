@@ -80,6 +80,45 @@ def test_noalloc_reads_caller_built_cross_section_tables():
     assert st == st_ref
 
 
+def test_noalloc_honours_the_tune_variant_bits():
+    """Bit 1 evaluates the cross sections inline even for simulations that
+    carry a caller-built table; bit 0 runs the 48-register kernel.  Both
+    give the workspace run's tallies under the same bits."""
+    b = engine.Batch(SIMS, seed=23)
+    keep = [engine.use_sigma_table(b._sims_arr[k], b.mats[b._idx[0][k]]) for k in range(b.n)]
+    assert sum(t is not None for t in keep) == 3
+    for variant in (2, 3):
+        tune = _lib.Tune(256, 0, 1, variant, 0)
+        ref, st_ref = b.run(tune)          # the workspace ignores sigma_table: its own tables or inline
+        got, st = _noalloc(b, tune)
+        _same(got, ref)
+        assert st == st_ref
+    with pytest.raises(_lib.MCDError):
+        _noalloc(b, _lib.Tune(512, 0, 1, 1, 0))     # the 48-register kernel takes at most 256 threads
+
+
+def test_noalloc_at_its_limit_of_64_simulations():
+    """Exactly MCD_STATIC_MAX_SIMS simulations fill the static array and the
+    largest shared-memory layout; a few electrons each, two calls in a row,
+    against the workspace run."""
+    sims = []
+    for k in range(_lib.STATIC_MAX_SIMS):
+        m = ("Al", "Si", "Cu", "Au")[k % 4]
+        E0 = (5000.0, 10000.0, 20000.0, 30000.0)[(k // 4) % 4]
+        tilt = (0.0, 20.0, 45.0, 70.0)[k // 16]
+        mode = "cont" if k % 9 == 4 else "DS"
+        sims.append(dict(input_par(m, E0, 1000.0, tilt, mode=mode, bethe="JL"), num_el=3 + (k * 7) % 11))
+    tune = _lib.Tune(256, 0, 1, 2, 0)
+    b = engine.Batch(sims, seed=29)
+    ref, st_ref = b.run(tune)
+    for _ in range(2):
+        got, st = _noalloc(b, tune)
+        _same(got, ref)
+        assert st == st_ref
+    for t, s in zip(got, sims):
+        assert sum(t[o] for o in ("bks", "abs", "trsm", "long")) == s["num_el"]
+
+
 def test_noalloc_rejects_too_many_simulations():
     b = engine.Batch(SIMS[:1], seed=1)
     n = _lib.STATIC_MAX_SIMS + 1
