@@ -1,8 +1,10 @@
 """Shared helpers of the GPU tests: run the CUDA path and the C oracle on the
 same inputs (same Philox stream, same tables copied back from the GPU)."""
 import math
+import os
 
 import numpy as np
+from scipy import stats
 
 import coracle
 import mcd_oracle as O
@@ -63,3 +65,74 @@ def eta_z(n1, k1, n2, k2):
 def theta_deg(c2):
     c2 = np.clip(np.asarray(c2, dtype=np.float64), 0.0, 1.0)
     return np.degrees(2.0 * np.arccos(np.sqrt(c2)))
+
+
+# ---------------------------------------------------------------------------
+# the three FP32 DS code paths the statistical tests pin to the reference
+# ---------------------------------------------------------------------------
+# plain_inline     one launch, every cross section evaluated per event
+# plain_tabulated  one launch reading the simulation's cross-section table
+# batched          the benchmarked configuration: the persistent kernel with
+#                  the tables mcd_batch_prepare builds (tune variant 0), block
+#                  1024, refill 1; one simulation with sim id 0, so it draws
+#                  the same Philox words as the plain launches
+VARIANTS = ("plain_inline", "plain_tabulated", "batched")
+BENCH_TUNE = (1024, 0, 1, 0, 0)
+
+
+def run_variant(variant, p, n, seed, electrons=True, ring_capacity=0, ring_fields=0):
+    """One FP32 run of n electrons of p on a code path of VARIANTS."""
+    if variant in ("plain_inline", "plain_tabulated"):
+        return engine.run(p, num_el=n, seed=seed, precision="fp32", electrons=electrons,
+                          ring_capacity=ring_capacity, ring_fields=ring_fields,
+                          tabulated=variant == "plain_tabulated")
+    if variant != "batched":
+        raise ValueError(variant)
+    b = engine.Batch([dict(p, num_el=n)], seed=seed, electrons=electrons)
+    tune = _lib.Tune(*BENCH_TUNE)
+    events, total = None, 0
+    if ring_capacity:
+        tallies, status, events, total = b.run_events(ring_capacity, fields=ring_fields, tune=tune)
+    else:
+        tallies, status = b.run(tune)
+    rows = b.electrons(0) if electrons else None
+    return engine.RunResult(tallies[0], status, rows, events, total)
+
+
+# ---------------------------------------------------------------------------
+# a rule for many independent tests at the p > 0.01 level
+# ---------------------------------------------------------------------------
+P_MIN = 0.01
+K_SUB = 10
+
+
+def max_rejections(k=K_SUB, p=P_MIN, q=0.999):
+    """The 99.9% quantile of Binomial(k, p): with no real difference, more
+    than this many of k independent tests at level p reject with probability
+    below 1e-3 (k = 10, p = 0.01: 2)."""
+    return int(stats.binom.ppf(q, k, p))
+
+
+def assert_subsamples(pvalues, what=""):
+    """K independent subsamples, each tested at p > P_MIN: fail when more of
+    them reject than chance allows (max_rejections)."""
+    pv = [float(x) for x in pvalues]
+    bad = sum(x <= P_MIN for x in pv)
+    assert bad <= max_rejections(len(pv)), (what, bad, ["%.3g" % x for x in pv])
+
+
+# ---------------------------------------------------------------------------
+# oracle tables on the reference's own grids (tests/golden/tables.npz)
+# ---------------------------------------------------------------------------
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def oracle_tables_from_golden(key):
+    """The oracle's FP64-filled tables (stored as float32, as the reference
+    stores them) on the W/E grids the reference's grid search chose for
+    table configuration `key` (e.g. 'cfg4_Al_5')."""
+    T = np.load(os.path.join(GOLDEN_DIR, "tables.npz"))
+    sp = str(T[key + "/Moller/species"])
+    mat = O.Material(sp)
+    return mat, [coracle.HostTable.build(kind, mat, T["%s/%s/Ws" % (key, kind)], T["%s/%s/Es" % (key, kind)])
+                 for kind in ("Moller", "Gryz")]

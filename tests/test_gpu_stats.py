@@ -3,13 +3,18 @@
 kinds of statistical checks as the reference's tests/testThings.py (channel
 mix at E0 by chi^2, polar and azimuthal angles, per-channel energy losses),
 plus backscatter coefficient eta within 3 sigma and KS tests on exit
-energies, exit angles, event counts and maximum depth, all at p > 0.01."""
+energies, exit angles, event counts and maximum depth, all at p > 0.01.
+
+Every check runs on each FP32 code path: the plain launch with cross
+sections evaluated per event, the plain launch reading its cross-section
+table, and the persistent batched kernel in the configuration the benchmark
+times (tabulated cross sections, block 1024, refill 1)."""
 import numpy as np
 import pytest
 from scipy import stats
 
-from mcd import _lib, engine
-from _gpu_util import eta_z, input_par, theta_deg
+from mcd import _lib
+from _gpu_util import VARIANTS, eta_z, input_par, run_variant, theta_deg
 
 pytestmark = pytest.mark.gpu
 
@@ -24,17 +29,21 @@ P_MIN = 0.01
 
 @pytest.fixture(scope="module")
 def runs():
-    out = {}
-    for tag, p in STATS.items():
-        n = 100000 if tag != "au30" else 20000
-        out[tag] = engine.run(p, num_el=n, seed=2024, precision="fp32")
-    return out
+    cache = {}
+
+    def get(variant, tag):
+        if (variant, tag) not in cache:
+            n = 100000 if tag != "au30" else 20000
+            cache[(variant, tag)] = run_variant(variant, STATS[tag], n, seed=2024)
+        return cache[(variant, tag)]
+    return get
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("tag", list(STATS))
-def test_eta_and_exit_distributions(golden, runs, tag):
+def test_eta_and_exit_distributions(golden, runs, tag, variant):
     S = golden["ref_stats"]
-    g = runs[tag]
+    g = runs(variant, tag)
     e = g.electrons
     n = e["outcome"].size
     ro = S[tag + "/outcome"]
@@ -54,14 +63,15 @@ def test_eta_and_exit_distributions(golden, runs, tag):
     assert abs(rate - rate_ref) < 3 * np.sqrt(max(rate_ref, 1e-4) * (1.0 / ro.size + 1.0 / n)) + 1e-4
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("tag", ["si10", "cu20t45", "al5"])
-def test_first_event_channels_and_angles(golden, tag):
+def test_first_event_channels_and_angles(golden, tag, variant):
     """Events at E0 (the first event of each electron): channel mix by chi^2,
     Rutherford polar angle and Moller energy loss by KS, azimuth uniform."""
     S = golden["ref_stats"]
     p = STATS[tag]
     n = 20000
-    g = engine.run(p, num_el=n, seed=99, precision="fp32", ring_capacity=n * 1200)
+    g = run_variant(variant, p, n, seed=99, electrons=False, ring_capacity=n * 1200)
     assert not (g.status & _lib.FLAG_RING_FULL)
     ev = g.events
     first = ev[(ev["step_chan"] >> 5) == 0]
@@ -91,15 +101,17 @@ def test_first_event_channels_and_angles(golden, tag):
     assert stats.kstest(phi / (2 * np.pi), "uniform").pvalue > P_MIN
 
 
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("tag", ["si10", "cu20t45"])
-def test_all_energy_samples(golden, tag):
+def test_all_energy_samples(golden, tag, variant):
     """Every-128th event of the reference against every-128th event here:
     Rutherford polar angle and inelastic energy losses over all energies
     (reference TestPolarProb_Ruth / TestPolarProb_Moller)."""
     S = golden["ref_stats"]
     p = STATS[tag]
     n = 16000
-    g = engine.run(p, num_el=n, seed=5, precision="fp32", ring_capacity=n * 1200)
+    g = run_variant(variant, p, n, seed=5, electrons=False, ring_capacity=n * 1200)
+    assert not (g.status & _lib.FLAG_RING_FULL)
     ev = g.events
     ev = ev[np.lexsort(((ev["step_chan"] >> 5), ev["electron"]))]
     steps = ev["step_chan"] >> 5

@@ -1,0 +1,104 @@
+"""The benchmarked workload, pinned statistically: all 64 DS simulations of
+the batched benchmark ({Al,Si,Cu,Au} x E0 {5,10,20,30} keV x tilt
+{0,20,45,70} deg, Emin 1 keV, Wc 100 eV, tol 1e-3) at min(num_el, 2000)
+electrons, run as one persistent launch in the configuration the benchmark
+times (tabulated cross sections, block 1024, refill 1), against the FP64
+C oracle on its own tables (the reference's W/E grids from
+tests/golden/tables.npz) and an independent Philox seed:
+  * eta of every simulation within 3 sigma, Bonferroni-adjusted over the 64
+    simulations (two-sided family level 0.0027, |z| < 4.01 each);
+  * KS at p > 0.01 of the exit energy and of the polar exit angle of the
+    backscattered electrons pooled over the 64 simulations (both sides hold
+    the same electron count per simulation, so both pools sample the same
+    mixture), and of the event counts per electron."""
+import math
+
+import numpy as np
+import pytest
+from scipy import stats
+
+import coracle
+from mcd import _lib, engine
+from _gpu_util import BENCH_TUNE, P_MIN, eta_z, oracle_tables_from_golden
+
+pytestmark = pytest.mark.gpu
+
+MATERIALS = ("Al", "Si", "Cu", "Au")
+ENERGIES = (5000.0, 10000.0, 20000.0, 30000.0)
+TILTS = (0.0, 20.0, 45.0, 70.0)
+N_CAP = 2000
+Z_MAX = stats.norm.isf(0.0027 / 2 / 64)
+
+
+def workload():
+    """The benchmark's 64 simulations (num_el = round(10^U[3,6]) from
+    default_rng(0) in this nested order), capped at N_CAP electrons."""
+    rng = np.random.default_rng(0)
+    sims = []
+    for m in MATERIALS:
+        for E0 in ENERGIES:
+            for t in TILTS:
+                n = int(round(10 ** rng.uniform(3, 6)))
+                sims.append(dict(material=m, E0=E0, Emin=1000.0, s_tilt=t, Wc=100.0, tol_E=1e-3, tol_W=1e-3,
+                                 mode="DS", num_el=min(n, N_CAP)))
+    return sims
+
+
+@pytest.fixture(scope="module")
+def pair():
+    sims = workload()
+    b = engine.Batch(sims, seed=7, electrons=True)
+    tallies, status = b.run(_lib.Tune(*BENCH_TUNE))
+    assert status & ~_lib.FLAG_NAN == 0, status
+    gpu = [b.electrons(k) for k in range(len(sims))]
+    ora, tabs = [], {}
+    for k, s in enumerate(sims):
+        key = "cfg4_%s_%d" % (s["material"], int(s["E0"] / 1000))
+        if key not in tabs:
+            tabs[key] = oracle_tables_from_golden(key)
+        mat, ht = tabs[key]
+        ora.append(coracle.run(mat, s["E0"], s["Emin"], s["s_tilt"], s["num_el"], seed=8, mode="DS", Wc=s["Wc"],
+                               tables=ht, sim_id=k, max_scatt=10 ** 6))
+    return sims, tallies, gpu, ora
+
+
+def test_every_simulation_runs_every_electron(pair):
+    sims, tallies, gpu, _ = pair
+    for s, t, g in zip(sims, tallies, gpu):
+        assert sum(t[o] for o in ("bks", "abs", "trsm", "trdf", "long")) == s["num_el"]
+        assert t["events"] == int(g["n_events"].sum())
+        assert t["bks"] == int((g["outcome"] == 1).sum())
+
+
+def test_eta_of_each_simulation_within_3_sigma_bonferroni(pair):
+    sims, _, gpu, ora = pair
+    zs = []
+    for s, g, c in zip(sims, gpu, ora):
+        n = s["num_el"]
+        zs.append(eta_z(n, int((g["outcome"] == 1).sum()), n, int((c["outcome"] == 1).sum())))
+    worst = int(np.argmax(zs))
+    assert max(zs) < Z_MAX, (sims[worst], zs[worst])
+    # and no drift shared by all simulations: the z values of 64 independent
+    # comparisons, signed, average to about 0
+    signed = []
+    for s, g, c in zip(sims, gpu, ora):
+        n = s["num_el"]
+        k1, k2 = int((g["outcome"] == 1).sum()), int((c["outcome"] == 1).sum())
+        p = (k1 + k2) / (2 * n)
+        signed.append(0.0 if p in (0.0, 1.0) else (k1 - k2) / n / math.sqrt(2 * p * (1 - p) / n))
+    assert abs(np.mean(signed)) * math.sqrt(len(signed)) < 3.0, np.mean(signed)
+
+
+def test_pooled_exit_distributions(pair):
+    _, _, gpu, ora = pair
+    gb = [g["outcome"] == 1 for g in gpu]
+    ob = [c["outcome"] == 1 for c in ora]
+    gE = np.concatenate([g["final_E"][m] for g, m in zip(gpu, gb)])
+    oE = np.concatenate([c["final_E"][m] for c, m in zip(ora, ob)])
+    assert stats.ks_2samp(gE, oE).pvalue > P_MIN
+    gT = np.concatenate([np.degrees(np.arccos(np.clip(-g["dir"][m, 2], -1, 1))) for g, m in zip(gpu, gb)])
+    oT = np.concatenate([np.degrees(np.arccos(np.clip(-c["dir"][m, 2], -1, 1))) for c, m in zip(ora, ob)])
+    assert stats.ks_2samp(gT, oT).pvalue > P_MIN
+    gN = np.concatenate([g["n_events"] for g in gpu])
+    oN = np.concatenate([c["n_events"] for c in ora])
+    assert stats.ks_2samp(gN, oN).pvalue > P_MIN
