@@ -10,10 +10,12 @@ path makes 64 launches of one thread per electron.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mcd|reference]
 
 Prints one JSON line (rank 0).  Under torchrun each rank runs the whole
-workload on its own electron indices (weak scaling, no data-path collective;
-the ranks only meet at the timing barrier).  --impl reference times the CPU
-restatement of the reference (the C oracle) on all host cores over a bounded
-sample of the same workload.
+workload on its own electron indices (weak scaling, no data-path
+collective): the ranks meet at the timing barrier, and after the timed
+region one sum of the tallies gives the whole job's event counts.
+--impl reference times the CPU restatement of the reference (the C oracle)
+on all host cores over a bounded, num_el-weighted sample of the same
+workload, on the reference's own W/E grids, without loading the library.
 """
 import argparse
 import json
@@ -41,7 +43,9 @@ N_SHELLS = {"Al": 3, "Si": 3, "Cu": 4, "Au": 8}
 # (FMA = 2) and special-function (MUFU) operations.
 FLOP_PER_EVENT = {k: 176 + 18 * n for k, n in N_SHELLS.items()}   # Si 230, Au 320
 MUFU_PER_EVENT = {k: 17 + 4 * n for k, n in N_SHELLS.items()}     # Si 29, Au 49
-CPU_SAMPLE_PER_SIM = 600
+# electrons of the bounded CPU sample, spread over the 64 simulations in
+# proportion to num_el, so that its mix of trajectory lengths is the workload's
+CPU_SAMPLE_ELECTRONS = 40000
 # DRAM bytes (read + write) of one batched launch of the 64-simulation step,
 # from an ncu capture of that launch (tables and workspace read about once;
 # the figure does not grow with the electrons)
@@ -149,20 +153,38 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(sims, per_sim, steps=1, seed=0):
-    """The C oracle over min(num_el, per_sim) electrons of every simulation."""
+def sample_sizes(sims, electrons=CPU_SAMPLE_ELECTRONS):
+    """Electrons of each simulation in a bounded CPU sample weighted like the
+    workload: num_el x (electrons / total electrons), at least one."""
+    total = sum(s["num_el"] for s in sims)
+    return [max(1, int(round(s["num_el"] * electrons / total))) for s in sims]
+
+
+def oracle_tables(s):
+    """The oracle's CDF tables of a workload simulation, on the W and E grids
+    the reference's own grid search chose for it (tests/golden/tables.npz,
+    written by tests/golden/gen_golden.py from the reference).  The CPU legs
+    load nothing of the library under test."""
     import coracle
     import mcd_oracle as O
-    from mcd import _lib, tables
+    mat = O.Material(s["material"])
+    T = np.load(os.path.join(ROOT, "tests", "golden", "tables.npz"))
+    key = "cfg4_%s_%d" % (s["material"], int(s["E0"] / 1000))
+    spec = T[key + "/Moller/spec"]
+    assert (spec[1], spec[2], spec[3]) == (s["Emin"], s["Wc"], s["tol_E"]), key
+    return mat, [coracle.HostTable.build(kind, mat, T["%s/%s/Ws" % (key, kind)], T["%s/%s/Es" % (key, kind)])
+                 for kind in ("Moller", "Gryz")]
+
+
+def cpu_sample(sims, sizes, steps=1, seed=0):
+    """The C oracle over the first sizes[k] electrons of simulation k (the
+    GPU's Philox electron indices and sim ids), on every host thread."""
+    import coracle
     threads = os.cpu_count() or 1
     prepared = []
-    for k, s in enumerate(sims):
-        mat = O.Material(s["material"])
-        m = _lib.material(s["material"])
-        ht = [coracle.HostTable.build(kind, mat, *tables.find_grids(kind, m, s["E0"], s["Emin"], s["Wc"],
-                                                                     s["tol_E"], s["tol_W"]))
-              for kind in ("Moller", "Gryz")]
-        prepared.append((mat, ht, min(per_sim, s["num_el"])))
+    for s, n in zip(sims, sizes):
+        mat, ht = oracle_tables(s)
+        prepared.append((mat, ht, min(n, s["num_el"])))
     times, events, electrons, bks, ns = [], 0, 0, [], []
     for _ in range(steps):
         t0 = time.perf_counter()
@@ -245,30 +267,57 @@ def cfg1_bench(args, dev):
             "identical_trajectories": same, "gpu_launches": 2 * max(3, args.steps)}
 
 
+def bench_config(sims):
+    """The workload as both arms name it (identical dicts)."""
+    return {"workload": WORKLOAD_NAME, "sims": len(sims),
+            "electrons_per_replica": sum(s["num_el"] for s in sims),
+            "l2": "GPU arm: flushed between timed steps (256 MB write)"}
+
+
+def reference_python_record():
+    """The reference's own Python DS worker (multiTraj_DS), timed where the
+    reference is installed (tests/golden/time_reference.py writes the
+    record); it cannot run on a host without the reference."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "reference_timing.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def sample_note(r):
+    return ("num_el-weighted sample: %d electrons over the 64 sims (num_el x %.3g, at least 1), %d events per "
+            "step, first electrons of each sim on the GPU's Philox indices"
+            % (r["electrons"], CPU_SAMPLE_ELECTRONS / max(1, r["total"]), r["events"]))
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     sims = workload()
+    sizes = sample_sizes(sims)
     # warm-up steps run a smaller slice of the same sample
     if args.warmup:
-        cpu_sample(sims[:4], CPU_SAMPLE_PER_SIM // 4, steps=args.warmup)
-    r = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=args.steps)
+        cpu_sample(sims[:8], sizes[:8], steps=args.warmup)
+    r = cpu_sample(sims, sizes, steps=args.steps)
+    r["total"] = sum(s["num_el"] for s in sims)
     t = sum(r["times"])
     v = r["events"] * len(r["times"]) / t
-    sample = ("min(num_el, %d) electrons of each of the 64 sims (%d electrons, %d events per step)"
-              % (CPU_SAMPLE_PER_SIM, r["electrons"], r["events"]))
+    sample = sample_note(r)
     line = {
         "impl": "reference", "metric": "scatter events/s", "value": v, "unit": "events/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(r["times"]),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD_NAME, "sample": sample},
+        "data": "synthetic", "config": bench_config(sims),
         "cpu_baseline": {"value": v, "unit": "events/s", "cores": r["threads"], "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "electrons_per_s": r["electrons"] * len(r["times"]) / t,
+        "reference_python": reference_python_record(),
         "note": "C restatement of the reference's DS trajectory loop (oracle/mcd_oracle.c), FP64, all host "
-                "threads; the reference itself is Python and is not present on the GPU host",
+                "threads, on the reference's own W/E grids; the reference itself is Python and is not present "
+                "on the GPU host (reference_python: its worker timed where it is installed)",
     }
     print(json.dumps(line), flush=True)
 
@@ -355,6 +404,63 @@ def adjoint_depth_bench(args, dev, p, n):
             "dL_dJscale": dJ, "dL_dnscale": dn, "fd_frozen_rel_err_J": abs(dJ - fdJ) / abs(fdJ) if fdJ else None,
             "fd_frozen_rel_err_n": abs(dn - fdn) / abs(fdn) if fdn else None, "fd_step": d,
             "gpu_launches": 2 * args.steps}
+
+
+TABLES_WORKLOAD = ("the sampled-loss table pairs (Moller, outermost-shell Gryzinski) of the 16 (material, E0) "
+                   "pairs of the 64-simulation workload (tol 1e-3), and of Au 30 keV, Emin 0.5 keV, Wc 50 eV, "
+                   "tol 1e-4: host grid search (QUADPACK reference integral, float32 trapezoid scans) and GPU FP64 "
+                   "fill with guide tables")
+
+
+def tables_bench(args, dev):
+    """Wall time of building the DS tables from scratch for a fresh parameter
+    set: the grid search on the host and the fill on the GPU (grid copies,
+    allocation and mcd_build_table, CUDA events), each table built twice and
+    the second build timed.  Beside them, the reference's own table build
+    (tests/golden/reference_timing.json: probTable grid search + computeBlock
+    per table, where the reference is installed)."""
+    import torch
+    from mcd import _lib, tables
+    stream = torch.cuda.current_stream(dev)
+
+    def build(sp, E0, Emin, Wc, tol):
+        m = _lib.material(sp)
+        t0 = time.perf_counter()
+        grids = [tables.find_grids(kind, m, E0, Emin, Wc, tol, tol) for kind in ("Moller", "Gryz")]
+        host = time.perf_counter() - t0
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t1 = time.perf_counter()
+        e0.record(stream)
+        dts = [tables.DeviceTable(kind, m, W, E, dev) for kind, (W, E) in zip(("Moller", "Gryz"), grids)]
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t1
+        cells = sum(d.nE * (d.nW - 1) for d in dts)
+        return host, e0.elapsed_time(e1) * 1e-3, wall, cells
+
+    pairs = sorted({(s["material"], s["E0"]) for s in workload()})
+    for sp, E0 in pairs[:2]:
+        build(sp, E0, 1000.0, 100.0, 1e-3)          # warm-up: imports, allocator
+    res = [build(sp, E0, 1000.0, 100.0, 1e-3) for sp, E0 in pairs]
+    au = build("Au", 30000.0, 500.0, 50.0, 1e-4)
+    au = build("Au", 30000.0, 500.0, 50.0, 1e-4)
+    ref = reference_python_record()
+    rt = ref["tables"] if ref else None
+    out = {"workload": TABLES_WORKLOAD,
+           "workload_16_pairs": {"host_search_ms": 1e3 * sum(r[0] for r in res),
+                                 "gpu_fill_ms": 1e3 * sum(r[1] for r in res),
+                                 "fill_wall_ms": 1e3 * sum(r[2] for r in res),
+                                 "total_ms": 1e3 * sum(r[0] + r[2] for r in res),
+                                 "cdf_cells": sum(r[3] for r in res),
+                                 "reference_s": rt["workload_total_s"] if rt else None},
+           "au30_tol1e-4": {"host_search_ms": 1e3 * au[0], "gpu_fill_ms": 1e3 * au[1], "fill_wall_ms": 1e3 * au[2],
+                            "total_ms": 1e3 * (au[0] + au[2]), "cdf_cells": au[3],
+                            "reference_s": rt["au30_tol1e-4_total_s"] if rt else None},
+           "reference_note": ("the reference's probTable grid search + computeBlock + memmap per table, one core of "
+                              "%s (%s)" % (ref["host"]["processor"], ref["date"])) if ref else None,
+           "gpu_launches": 2 * (len(res) + 2 + 2)}
+    return out
 
 
 CONT_WORKLOAD = ("continuous JL Bethe, Cu, E0 20 keV, Emin 1 keV, tilt 70 deg, 1e6 electrons, FP32; "
@@ -612,11 +718,12 @@ def run_mcd(args):
     clk = clocks.stop()
     k_plain = max(1, args.steps // 2)
     if args.no_plain:
-        t_plain, t_plain_inline, ptallies = float("nan"), float("nan"), tallies
+        t_plain, t_plain_inline, ptallies, pitallies = float("nan"), float("nan"), tallies, tallies
     else:
         t_plain = timed(plain_step, k_plain)
         ptallies = [engine.collect(b[3]).tally for b in plain]
         t_plain_inline = timed(plain_inline_step, k_plain)
+        pitallies = [engine.collect(b[3]).tally for b in plain_inline]
     barrier()
 
     # end to end through the public API: host-side inputs packed and copied
@@ -636,6 +743,19 @@ def run_mcd(args):
     e2e_tallies = [engine.tally_from_bytes(host_t[k].numpy()) for k in range(batch.n)]
     assert sum(t["events"] for t in e2e_tallies) == events
 
+    def summed(tl):
+        """Tallies summed over the ranks (each rank transported its own
+        electrons): one collective of the integer counts, one of the FP64 sums."""
+        if dist is None:
+            return tl
+        v = torch.from_numpy(np.stack([shard.tally_vector(t) for t in tl])).to(dev)
+        s = torch.tensor([[t[k] for k in shard.SUM_KEYS] for t in tl], dtype=torch.float64, device=dev)
+        dist.all_reduce(v)
+        dist.all_reduce(s)
+        return [shard.tally_from_vector(a, dict(zip(shard.SUM_KEYS, b)))
+                for a, b in zip(v.cpu().numpy(), s.cpu().numpy())]
+
+    tallies, ptallies, pitallies = summed(tallies), summed(ptallies), summed(pitallies)
     if dist is not None:
         tt = torch.tensor([t_batched, t_plain, t_plain_inline, t_e2e], dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -645,9 +765,12 @@ def run_mcd(args):
         return
 
     K = args.steps
-    value = events * ws * K / t_batched
-    plain_value = events * ws * k_plain / t_plain
-    plain_inline_value = events * ws * k_plain / t_plain_inline
+    # every count below is the sum over all ranks; times are the slowest rank's
+    events = sum(t["events"] for t in tallies)
+    electrons = sum(sum(t[o] for o in ("bks", "abs", "trsm", "trdf", "long")) for t in tallies)
+    value = events * K / t_batched
+    plain_value = sum(t["events"] for t in ptallies) * k_plain / t_plain
+    plain_inline_value = sum(t["events"] for t in pitallies) * k_plain / t_plain_inline
     # eta: batched vs plain (same counters) and vs the reference's samples
     zs = []
     for t, p in zip(tallies, ptallies):
@@ -679,42 +802,68 @@ def run_mcd(args):
     kt = t_batched / K
     fp32_peak = sms * 128 * 2 * fmax / 1e12
     mufu_peak = sms * 16 * fmax / 1e12
-    ach = flop / kt / 1e12
-    ach_mufu = mufu / kt / 1e12
+    ach = flop / kt / ws / 1e12          # per GPU
+    ach_mufu = mufu / kt / ws / 1e12
+    # the binding limit is the larger of the two fractions; both peaks are
+    # nominal formulas (the measured-peaks file holds HBM and bf16 GEMM rates)
+    fp32 = {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+            "per_event": "176 + 18 n_shells FLOP (FMA = 2)"}
+    mufu_ = {"achieved": ach_mufu, "peak": mufu_peak, "unit": "Tops/s", "frac": ach_mufu / mufu_peak,
+             "per_event": "17 + 4 n_shells MUFU operations"}
+    top, name = (mufu_, "mufu-issue") if mufu_["frac"] >= fp32["frac"] else (fp32, "fp32-issue")
+    roofline = {"bound": name, "achieved": top["achieved"], "peak": top["peak"], "unit": top["unit"],
+                "frac": top["frac"], "traffic": BATCHED_DRAM_BYTES if args.scale == 1.0 else None,
+                "traffic_note": "DRAM bytes per launch from an ncu capture of the full step",
+                "fp32": fp32, "mufu": mufu_,
+                "issue": {"achieved": value * WARP_INST_PER_EVENT / 1e9 / ws,
+                          "peak": sms * 4 * fmax / 1e9, "unit": "G warp instructions/s",
+                          "frac": value * WARP_INST_PER_EVENT / ws / (sms * 4 * fmax),
+                          "inst_per_event_note": "warp instructions per event from an ncu capture"},
+                "ncu": BATCHED_NCU,
+                "peak_note": "nominal peaks, not measured: %d SMs x 128 FP32 lanes x 2 FLOP (MUFU: x16 ops) per "
+                             "cycle at sm_max_mhz %.0f; frac is the larger of the FP32 and MUFU fractions"
+                             % (sms, fmax / 1e6)}
 
     adj = None if args.no_adjoint else adjoint_bench(args, dev)
     stream = None if args.no_stream else stream_bench(args, dev)
     cont = None if args.no_cont else cont_bench(args, dev)
     det = None if args.no_detector else detector_bench(args, dev)
+    tabs = None if args.no_tables else tables_bench(args, dev)
     if args.no_cpu:
-        cpu = {"events": 0, "times": [float("nan")], "threads": 0}
+        cpu = {"events": 0, "electrons": 0, "times": [float("nan")], "threads": 0, "total": 1}
     else:
-        cpu = cpu_sample(sims, CPU_SAMPLE_PER_SIM, steps=1, seed=args.seed)
+        cpu = cpu_sample(sims, sample_sizes(sims), steps=1, seed=args.seed)
+        cpu["total"] = sum(s["num_el"] for s in sims)
     cpu_v = cpu["events"] / cpu["times"][0]
-    # eta of every simulation against the FP64 oracle's sample of its first electrons
+    # eta against the FP64 oracle's sample of the first electrons of each
+    # simulation: pooled over the (num_el-weighted) sample, and per simulation
+    # where the sample holds at least 100 electrons
     vs_oracle = None
     if not args.no_cpu:
+        def z2(k1, n1, k2, n2):
+            pp = (k1 + k2) / (n1 + n2)
+            return abs(k1 / n1 - k2 / n2) / math.sqrt(max(pp * (1 - pp), 1e-12) * (1 / n1 + 1 / n2))
         zo = []
         for k, t in enumerate(tallies):
-            n = sum(t[o] for o in ("bks", "abs", "trsm", "long"))
-            k2, n2 = cpu["bks"][k], cpu["n"][k]
-            pp = (t["bks"] + k2) / (n + n2)
-            zo.append(abs(t["bks"] / n - k2 / n2) / math.sqrt(max(pp * (1 - pp), 1e-12) * (1 / n + 1 / n2)))
-        vs_oracle = {"max_z": max(zo), "mean_z": sum(zo) / len(zo), "sims": len(zo),
-                     "oracle_electrons_per_sim": "min(num_el, %d)" % CPU_SAMPLE_PER_SIM}
+            if cpu["n"][k] >= 100:
+                zo.append(z2(t["bks"], sum(t[o] for o in ("bks", "abs", "trsm", "long")), cpu["bks"][k], cpu["n"][k]))
+        ng = sum(sum(t[o] for o in ("bks", "abs", "trsm", "long")) for t in tallies)
+        vs_oracle = {"pooled_z": z2(sum(t["bks"] for t in tallies), ng, sum(cpu["bks"]), sum(cpu["n"])),
+                     "eta_gpu": sum(t["bks"] for t in tallies) / ng, "eta_oracle": sum(cpu["bks"]) / sum(cpu["n"]),
+                     "max_z": max(zo) if zo else None, "sims_with_100": len(zo),
+                     "oracle_sample": sample_note(cpu)}
     c1 = None if args.no_cfg1 else cfg1_bench(args, dev)
 
     line = {
         "metric": "scatter events/s", "value": value, "unit": "events/s", "n_gpus": ws, "steps": K,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_batched / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD_NAME, "sims": len(sims), "electrons_per_step": electrons * ws,
-                   "events_per_step": events * ws,
-                   "tune": {"block": tune.block_size, "refill": tune.refill, "variant": tune.variant,
-                            "blocks_per_sm": tune.blocks_per_sm,
-                            "autotuned_ms": tune_table, "cuda_graph": True},
-                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas" if ws > 1 else "1 GPU"},
-        "electrons_per_s": electrons * ws * K / t_batched,
+        "config": bench_config(sims),
+        "electrons_per_step": electrons, "events_per_step": events,
+        "parallelism": "%d replicas, counts summed over ranks" % ws if ws > 1 else "1 GPU",
+        "tune": {"block": tune.block_size, "refill": tune.refill, "variant": tune.variant,
+                 "blocks_per_sm": tune.blocks_per_sm, "autotuned_ms": tune_table, "cuda_graph": True},
+        "electrons_per_s": electrons * K / t_batched,
         "plain": {"value": plain_value, "unit": "events/s", "ms_per_step": 1e3 * t_plain / k_plain,
                   "launches_per_step": len(sims), "cross_sections": "one table per simulation"},
         "plain_inline": {"value": plain_inline_value, "unit": "events/s",
@@ -723,27 +872,19 @@ def run_mcd(args):
         "batched_over_plain": value / plain_value,
         "batched_over_plain_inline": value / plain_inline_value,
         "eta": {"batched_vs_plain_max_z": max(zs), "vs_reference": ref, "vs_oracle_fp64": vs_oracle},
-        "e2e": {"value": events * ws * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": int(_lib.lib().mcd_batch_upload_bytes(batch.n)),
+        "e2e": {"value": events * K / t_e2e, "unit": "events/s", "h2d_bytes_per_step": int(_lib.lib().mcd_batch_upload_bytes(batch.n)),
                 "d2h_bytes_per_step": int(batch.tallies.numel())},
-        "roofline": {"bound": "fp32-issue", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": ach / fp32_peak, "traffic": BATCHED_DRAM_BYTES if args.scale == 1.0 else None,
-                     "traffic_note": "DRAM bytes per launch from an ncu capture of the full step",
-                     "mufu": {"achieved": ach_mufu, "peak": mufu_peak, "unit": "Tops/s", "frac": ach_mufu / mufu_peak},
-                     "issue": {"achieved": value * WARP_INST_PER_EVENT / 1e9 / ws,
-                               "peak": sms * 4 * fmax / 1e9, "unit": "G warp instructions/s",
-                               "frac": value * WARP_INST_PER_EVENT / ws / (sms * 4 * fmax),
-                               "inst_per_event_note": "warp instructions per event from an ncu capture"},
-                     "ncu": BATCHED_NCU,
-                     "peak_note": "nominal %d SMs x 128 FP32 lanes x 2 (MUFU: x16) at sm_max_mhz %.0f" % (sms, fmax / 1e6)},
+        "roofline": roofline,
         "cpu_baseline": {"value": cpu_v, "unit": "events/s", "cores": cpu["threads"], "kind": "port",
-                         "sample": "C oracle, min(num_el, %d) electrons of each sim (%d events)"
-                                   % (CPU_SAMPLE_PER_SIM, cpu["events"])},
+                         "sample": "C oracle, " + sample_note(cpu) if cpu["electrons"] else None},
+        "reference_python": reference_python_record(),
         "clocks": clk,
         "adjoint": adj,
         "stream": stream,
         "cont": cont,
         "cfg1": c1,
         "detector": det,
+        "tables": tabs,
         "gpu_launches": K,
         "status": status,
     }
@@ -771,6 +912,7 @@ def main():
     ap.add_argument("--no-cont", action="store_true", help="skip the continuous-mode histogram measurement")
     ap.add_argument("--no-detector", action="store_true", help="skip the detector-projection measurement")
     ap.add_argument("--no-cfg1", action="store_true", help="skip the small FP64 configuration")
+    ap.add_argument("--no-tables", action="store_true", help="skip the table-build timing")
     ap.add_argument("--stream-fraction", type=float, default=1.0,
                     help="fraction of the 1e7-electron streaming workload to run (1 = all of it)")
     args = ap.parse_args()

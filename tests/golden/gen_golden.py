@@ -1,11 +1,12 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Runs only where the reference is mounted (read-only at /root/reference); the
-fixtures it writes are committed and the tests read those, so nothing on the
-GPU host needs the reference.  Usage:
+Runs only where a checkout of the reference exists, named by the
+MCD_REFERENCE_ROOT environment variable; the fixtures it writes are
+committed and the tests read those, so nothing on the GPU host needs the
+reference.  Usage:
 
-    python tests/golden/gen_golden.py physics tables replay     # seconds
-    python tests/golden/gen_golden.py stats                     # minutes
+    MCD_REFERENCE_ROOT=<checkout> python tests/golden/gen_golden.py physics tables replay   # seconds
+    MCD_REFERENCE_ROOT=<checkout> python tests/golden/gen_golden.py stats                   # minutes
 
 Parts:
   physics  material constants, total cross sections, stopping powers,

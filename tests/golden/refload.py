@@ -1,6 +1,7 @@
 """Import the reference's MC/tools modules in this container (fixture generation only).
 
-The reference is read from /root/reference (read-only).  Missing third-party
+The reference checkout is named by the MCD_REFERENCE_ROOT environment
+variable (the directory holding MC/tools).  Missing third-party
 modules are replaced by the stubs in tests/golden/refshim, and the two NumPy 2
 renames the reference still uses (np.trapz, np.NaN) are aliased.  The
 reference's table module configures logging to ../logs at import time, so the
@@ -13,8 +14,15 @@ import tempfile
 
 import numpy as np
 
-REF_ROOT = "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def ref_root():
+    root = os.environ.get("MCD_REFERENCE_ROOT")
+    if not root or not os.path.isdir(os.path.join(root, "MC", "tools")):
+        raise RuntimeError("set MCD_REFERENCE_ROOT to a checkout of the reference (the directory holding "
+                           "MC/tools)")
+    return root
 
 
 def load():
@@ -27,7 +35,7 @@ def load():
     if shim not in sys.path:
         sys.path.insert(0, shim)
     import quaternion  # noqa: F401  (registers np.quaternion)
-    mc = os.path.join(REF_ROOT, "MC")
+    mc = os.path.join(ref_root(), "MC")
     if mc not in sys.path:
         sys.path.insert(0, mc)
     scratch = tempfile.mkdtemp(prefix="mcref_")
