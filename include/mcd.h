@@ -152,12 +152,14 @@ typedef struct mcd_sim {
                                 and crossing the bottom face on that step is
                                 'trdf' (MC/tools/scattering.py:510-548,658-668,
                                 MC/tools/electron.py:72-79); needs xip_g > 0 */
-    const float* sigma_table;/* DS, FP32: device table from
-                                mcd_build_sigma_table for this simulation,
-                                read by mcd_run and mcd_run_batched_noalloc
-                                instead of evaluating the channel cross
-                                sections (NULL: evaluate them);
-                                mcd_batch_prepare builds its own tables      */
+    const void* sigma_table; /* DS: device table from mcd_build_sigma_table
+                                for this simulation (built for its
+                                precision: float for FP32 transport, double
+                                for FP64), read by mcd_run and (FP32)
+                                mcd_run_batched_noalloc instead of
+                                evaluating the channel cross sections
+                                (NULL: evaluate them); mcd_batch_prepare
+                                builds its own tables                       */
     const struct mcd_electron_out* electrons;
                              /* mcd_batch_prepare, mcd_run_batched_noalloc:
                                 this simulation's per-electron rows (device
@@ -274,17 +276,26 @@ int mcd_build_table(int kind, const mcd_material* mat, int shell,
                     float* cdf32, double* cdf64, int32_t* nvalid, uint16_t* guide,
                     void* stream);
 
-/* Cross-section table of one DS simulation, for mcd_sim.sigma_table: on a
- * log2-E grid of 128 points per octave over [Emin, E0], E times the total
- * channel cross section and E times the running sums in pick order (Ruth,
- * Moller, Gryzinski shells), FP64 evaluation of the expressions of
- * MC/tools/crossSections.py:37-284 stored as FP32 -- the table the batched
- * path builds per group of simulations.  It depends on the material, Wc,
- * the elastic model, n_scale, E0 and Emin.  table is device memory of
+/* Cross-section table of one DS simulation, for mcd_sim.sigma_table, built
+ * for the simulation's precision from the FP64 evaluation of the expressions
+ * of MC/tools/crossSections.py:37-284.
+ * FP32: on a log2-E grid of 128 points per octave over [Emin, E0], E times the
+ * total channel cross section and E times the running sums in pick order
+ * (Ruth, Moller, Gryzinski shells), stored as FP32 and interpolated
+ * linearly (within 3e-7 of the exact sums) -- the table the batched path
+ * builds per group of simulations.
+ * FP64: the same sums stored as FP64 on grids uniform in E inside each
+ * octave of (Emin, E0] (256 cells per octave, indexed from the exponent and
+ * mantissa bits of E), interpolated by the cubic through four nodes (within
+ * about 4e-10 of the exact sums); cells whose nodes straddle a channel
+ * threshold are flagged and evaluated exactly.  The octaves must fit the
+ * buffer: MCD_ETOOBIG otherwise (Au from 0.5 to 30 keV fits).
+ * It depends on the material, Wc, the elastic model, n_scale, E0, Emin and
+ * the precision.  table is 16-byte-aligned device memory of
  * mcd_sigma_table_bytes() bytes.                                            */
 size_t mcd_sigma_table_bytes(void);
 int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat,
-                          float* table, void* stream);
+                          void* table, void* stream);
 
 /* One simulation, one GPU thread per electron, one launch.
  * Replaces multiTraj_DS / multiTraj_cont (MC/tools/multiScatter.py:66-116,
@@ -292,10 +303,12 @@ int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat,
  * (MC/tools/singleScatter.py:10-41, 205-239).  moller/gryz are used in DS
  * mode only (gryz = the outermost shell's table, which samples every
  * Gryzinski loss, MC/tools/scattering.py:625).  electrons and ring may be
- * NULL.  tally and status are device pointers.  block_size is 8, 16 or a
- * multiple of 32 up to 256, or 0: 128, halved down to 8 while the grid would
- * leave SMs idle, so that a small job spreads over more SMs with fewer
- * lanes each (results do not depend on it).                                */
+ * NULL.  tally and status are device pointers.  block_size is 1, 2, 4, 8,
+ * 16 or a multiple of 32 up to 256, or 0: 128, halved down to 8 while the
+ * grid would leave SMs idle, so that a small job spreads over more SMs with
+ * fewer lanes each, and for FP64 transport further down to 2 while the grid
+ * stays within one warp per scheduler (results do not depend on it).  A DS
+ * simulation with a sigma_table reads its channel cross sections from it.  */
 int mcd_run(const mcd_sim* sim, const mcd_material* mat,
             const mcd_table* moller, const mcd_table* gryz,
             mcd_tally* tally, const mcd_electron_out* electrons,

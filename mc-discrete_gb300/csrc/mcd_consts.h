@@ -105,7 +105,11 @@ struct __align__(16) SimConst {
     // padding FLT_MAX).  The total and the first sums share one 16-byte load.
     // E * sigma varies slowly in log E, so linear interpolation at 128 rows
     // per octave is within 3e-7 of the exact sums (relative to the total).
-    const float* sig;
+    // FP64 transport reads an FP64 table (the octave blocks described at
+    // kSig64Cells) through the same pointer: sig_l0 then holds the first
+    // octave's exponent, sig_rows the number of octaves and sig_S the row
+    // stride in doubles (sig_K + 1, the flag last).
+    const void* sig;
     float sig_l0, sig_inv, sig_tmax, sig_off;   // sig_off = -sig_l0 * sig_inv
     int32_t sig_K, sig_S, sig_rows;
     // the small fields the event code tests, packed so that one load serves
@@ -126,6 +130,37 @@ __host__ __device__ __forceinline__ int bits_S(const C& c) { return (int)((c.bit
 constexpr int kSigRowsMax = 4096;      // grid points of a cross-section table, at most
 constexpr int kSigStride = 12;         // floats per row, at most (3 + MCD_MAX_SHELLS + 1)
 constexpr double kSigPerOctave = 128;  // grid density
+
+// FP64 cross-section tables (FP64 DS transport reading mcd_sim.sigma_table):
+// one block of kSig64Rows rows per octave [2^e, 2^(e+1)) of the energy range,
+// uniform in E inside the octave: kSig64Cells cells of 2^e / kSig64Cells eV,
+// with one node below the octave and two above it, so that the cubic
+// through the nodes i-1 .. i+2 (block rows i .. i+3) serves cell i.  A row
+// holds E times the total, E times the running sums in pick order (Ruth,
+// +Moller, +Gryz[k] ...), then a flag: 1 when a channel threshold (a shell's
+// binding energy, Wc, the plasmon energy) lies inside the cell's four-node
+// span, where the transport evaluates the cross sections instead (they have
+// a kink there).  The octave is the exponent of E and the position inside it
+// the mantissa, so the index needs no logarithm and is exact; the cubic is
+// within about 4e-10 of the exact sums (relative to the total) away from
+// thresholds for Al, Si, Cu and Au over 0.5-30 keV.
+constexpr int kSig64Cells = 256;
+constexpr int kSig64Rows = kSig64Cells + 3;
+
+// First octave exponent and octave count of an FP64 table over (lo, hi].
+inline int sigma_octaves64(double lo, double hi, int32_t* e_lo) {
+    int a = 0, b = 0;
+    frexp(lo, &a);   // lo = m 2^a with m in [0.5, 1): octave a - 1
+    frexp(hi, &b);
+    *e_lo = a - 1;
+    return b - a + 1;
+}
+
+// Bytes of the FP64 table of a simulation (K channel columns + the flag).
+inline size_t sigma_bytes64(double lo, double hi, int K) {
+    int32_t e0 = 0;
+    return sizeof(double) * (size_t)sigma_octaves64(lo, hi, &e0) * kSig64Rows * (size_t)(K + 1);
+}
 
 // The log2-E grid of a cross-section table over [lo, hi] (eV), slightly
 // widened so that both ends interpolate inside it.
@@ -235,8 +270,15 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     c.sig_rows = 0;
     if (s.sigma_table && s.mode == MCD_MODE_DS) {
         c.sig = s.sigma_table;
-        sigma_grid(s.Emin, s.E0, &c.sig_l0, &c.sig_inv, &c.sig_tmax, &c.sig_rows);
-        c.sig_off = -c.sig_l0 * c.sig_inv;
+        if (s.precision == MCD_FP64) {
+            int32_t e0 = 0;
+            c.sig_rows = sigma_octaves64(s.Emin, s.E0, &e0);
+            c.sig_l0 = (float)e0;
+            c.sig_S = c.sig_K + 1;
+        } else {
+            sigma_grid(s.Emin, s.E0, &c.sig_l0, &c.sig_inv, &c.sig_tmax, &c.sig_rows);
+            c.sig_off = -c.sig_l0 * c.sig_inv;
+        }
     }
     c.bits = (c.quirks & 7u) | (c.diff ? kBitDiff : 0u) | (c.mode == MCD_MODE_CONT ? kBitCont : 0u) |
              ((c.tally_flags & MCD_TALLY_CHANNELS) ? kBitChan : 0u) | (c.ruth_r2 ? kBitR2 : 0u) |
@@ -253,7 +295,12 @@ inline int check_sim(const mcd_sim& s, const mcd_material& m, const mcd_table* t
     if (s.precision != MCD_FP32 && s.precision != MCD_FP64) return MCD_EINVAL;
     if (s.elastic < MCD_ELASTIC_RUTH || s.elastic > MCD_ELASTIC_NIGRAM_WDEFL) return MCD_EINVAL;
     if (s.diff_mfp && (s.mode != MCD_MODE_DS || !(m.xip_g > 0))) return MCD_EINVAL;
-    if (s.sigma_table && (s.mode != MCD_MODE_DS || s.precision != MCD_FP32)) return MCD_EINVAL;
+    if (s.sigma_table && s.mode != MCD_MODE_DS) return MCD_EINVAL;
+    // an FP64 table must fit the mcd_sigma_table_bytes() a caller allocates
+    if (s.sigma_table && s.precision == MCD_FP64 && m.n_shells >= 0 && m.n_shells <= MCD_MAX_SHELLS &&
+        s.E0 > s.Emin && s.Emin > 0 &&
+        sigma_bytes64(s.Emin, s.E0, m.n_shells + 3) > sizeof(float) * (size_t)kSigRowsMax * kSigStride)
+        return MCD_ETOOBIG;
     if (!(s.E0 > s.Emin) || !(s.Emin > 0)) return MCD_EINVAL;
     if (s.num_el < 0) return MCD_EINVAL;
     if (m.n_shells < 0 || m.n_shells > MCD_MAX_SHELLS || m.atnd <= 0) return MCD_EINVAL;

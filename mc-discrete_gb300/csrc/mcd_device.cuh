@@ -74,14 +74,10 @@ struct Ops<double> {
     static __device__ __forceinline__ double ln(double x) { return log(x); }
     static __device__ __forceinline__ double ln_step(double x) { return log(x); }
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-    static __device__ __forceinline__ double rsqrt_(double x) { return 1.0 / sqrt(x); }
+    static __device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
     static __device__ __forceinline__ double div(double a, double b) { return a / b; }
     static __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
-    static __device__ __forceinline__ void sincos_pi(double u, double* s, double* c) {
-        const double a = 3.141592653589793 * u;
-        *s = sin(a);
-        *c = cos(a);
-    }
+    static __device__ __forceinline__ void sincos_pi(double u, double* s, double* c) { sincospi(u, s, c); }
     static __device__ __forceinline__ double nan_() { return __longlong_as_double(0x7ff8000000000000ll); }
     static __device__ __forceinline__ double acos_deg(double x) { return acos(x) * 57.29577951308232; }
 };
@@ -341,7 +337,7 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     const int i = (int)t;
     const float f = t - (float)i;
     const int S = bits_S(c);
-    const float* r0 = c.sig + i * S;
+    const float* r0 = static_cast<const float*>(c.sig) + i * S;
     const float* r1 = r0 + S;
     const int K = bits_K(c);
     // column 0 holds the total, columns 1.. the running sums before it
@@ -374,6 +370,50 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     return MCD_CH_GRYZ0 + (j - 2);
 }
 
+// The same from an FP64 table (FP64 transport; layout at kSig64Cells): the
+// octave block from the exponent bits of E, the cell and its offset from
+// the mantissa bits (exact), and the cubic through the cell's four nodes in
+// each column.  Returns -1 for a cell whose nodes straddle a channel
+// threshold (its flag is set): the caller evaluates the cross sections.
+template <class C>
+__device__ __forceinline__ int tab_pick64(const C& c, double E, double U, double* Etot_out) {
+    const long long b = __double_as_longlong(E);
+    const int ex = (int)((b >> 52) & 0x7ff) - 1023;
+    const double m = __longlong_as_double((b & 0x000fffffffffffffll) | 0x3ff0000000000000ll);   // [1, 2)
+    const double t = (m - 1.0) * (double)kSig64Cells;                                           // exact
+    int i = (int)t;
+    const double f = t - (double)i;
+    int blk = ex - (int)c.sig_l0;
+    blk = blk < 0 ? 0 : (blk > c.sig_rows - 1 ? c.sig_rows - 1 : blk);
+    i = i > kSig64Cells - 1 ? kSig64Cells - 1 : i;
+    const int S = bits_S(c), K = bits_K(c);
+    const double* r = static_cast<const double*>(c.sig) + ((size_t)blk * kSig64Rows + i) * S;
+    if (__ldg(r + K) != 0.0) return -1;
+    // Lagrange weights of the nodes at -1, 0, 1, 2 (in cells) for offset f
+    const double fp1 = f + 1.0, fm1 = f - 1.0, fm2 = f - 2.0;
+    const double w0 = -f * fm1 * fm2 * (1.0 / 6.0);
+    const double w1 = 0.5 * fp1 * fm1 * fm2;
+    const double w2 = -0.5 * fp1 * f * fm2;
+    const double w3 = fp1 * f * fm1 * (1.0 / 6.0);
+    auto at = [&](int col) {
+        return fma(w0, __ldg(r + col), fma(w1, __ldg(r + S + col), fma(w2, __ldg(r + 2 * S + col), w3 * __ldg(r + 3 * S + col))));
+    };
+    const double tot = at(0);
+    double all = tot;
+    if (c.bits & kBitDiff) all = fma(E, (double)c.dS, tot);   // + diffraction
+    *Etot_out = all;
+    const double target = U * all;
+    if ((c.bits & kBitDiff) && target > tot) return MCD_CH_DIFF;
+    // the first running sum at or above the target names the channel (most
+    // events stop at the Rutherford column)
+    int j = 0;
+    while (j < K - 1 && at(j + 1) < target) ++j;
+    if (j == 0) return MCD_CH_RUTH;
+    if (j == 1) return MCD_CH_MOLLER;
+    if (j == K - 1) return MCD_CH_QUINN;
+    return MCD_CH_GRYZ0 + (j - 2);
+}
+
 // Rutherford sin^2(theta/2) = a U / (a + 1 - U), a = a0 / E
 // (MC/tools/scattering.py:125-152); for the DS event in FP32 with one
 // division as a0 U / (a0 + E (1 - U)).
@@ -382,8 +422,7 @@ __device__ __forceinline__ T ruth_s2(const C& c, T E, uint32_t u) {
     if constexpr (sizeof(T) == 4) {
         return Ops<T>::div(c.a0 * Ops<T>::unit(u), fmaf(E, Ops<T>::unit_c(u), c.a0));
     } else {
-        const T a = Ops<T>::div(c.a0, E);
-        return Ops<T>::div(a * Ops<T>::unit(u), a + Ops<T>::unit_c(u));
+        return c.a0 * Ops<T>::unit(u) / fma(E, Ops<T>::unit_c(u), c.a0);
     }
 }
 
@@ -400,10 +439,18 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     int ch = MCD_CH_QUINN;
     T inv_tot;
     if (use_tab) {
-        float Etot;
-        ch = tab_pick(c, (float)E, (float)Ops<T>::unit(r.x), &Etot);
-        inv_tot = Ops<T>::div(E, (T)Etot);
-    } else {
+        if constexpr (sizeof(T) == 4) {
+            float Etot;
+            ch = tab_pick(c, (float)E, (float)Ops<T>::unit(r.x), &Etot);
+            inv_tot = Ops<T>::div(E, (T)Etot);
+        } else {
+            double Etot;
+            ch = tab_pick64(c, E, Ops<T>::unit(r.x), &Etot);
+            if (ch >= 0) inv_tot = E / Etot;
+            else use_tab = false, ch = MCD_CH_QUINN;   // a threshold inside the cell
+        }
+    }
+    if (!use_tab) {
         // --- cross sections, channel order Ruth, Moller, Gryz[k], Quinn
         const T invE = Ops<T>::div((T)1, E);
         const T sR = sig_ruth<T>(c, E);

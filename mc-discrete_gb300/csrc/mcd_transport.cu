@@ -117,8 +117,11 @@ __device__ __forceinline__ uint32_t finish_electron(const C& c, const Lane<T>& L
     return st;
 }
 
+// Called by every thread of the block; a block smaller than a warp (plain
+// launches of 1 to 16 threads) leaves lanes that never exist, so the
+// reduction names the lanes present.
 __device__ __forceinline__ void or_status(uint32_t* status, uint32_t st) {
-    const uint32_t w = __reduce_or_sync(0xffffffffu, st);
+    const uint32_t w = __reduce_or_sync(__activemask(), st);
     if ((threadIdx.x & 31) == 0 && w) atomicOr(status, w);
 }
 
@@ -139,7 +142,6 @@ __global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* 
     bt_zero(&bt, 1);
     __syncthreads();
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    constexpr bool kTab = sizeof(T) == 4;   // FP32 transport may read a cross-section table
     uint32_t st = 0;
     if (i < (uint64_t)c.num_el) {
         Lane<T> L;
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(256) k_plain(const SimConst<T> cp, mcd_tally* 
         const bool chan = (c.tally_flags & MCD_TALLY_CHANNELS) != 0;
         while (L.outcome == MCD_OUT_NONE) {
             EventOut<T> ev;
-            const int ch = (MODE == MCD_MODE_DS) ? ds_event<T, REC>(L, c, elec, &ev, kTab && c.sig != nullptr)
+            const int ch = (MODE == MCD_MODE_DS) ? ds_event<T, REC>(L, c, elec, &ev, c.sig != nullptr)
                                                  : cont_event<T, REC>(L, c, elec, &ev);
             if (ch >= 0) {
                 if (REC) st |= ring_append(ring, (uint32_t)i, L.step, ev);
@@ -397,6 +399,40 @@ __global__ void __launch_bounds__(256) k_sigtab_one(const SimConst<double> c, fl
     sig_row(c, l0, inv, S, i, table + (size_t)i * S);
 }
 
+// The FP64 table of one simulation (mcd_build_sigma_table for FP64
+// transport; layout at kSig64Cells): one thread per (octave block, row).
+// Block row q of octave e holds node q - 1 at E = 2^e (1 + (q - 1) / cells),
+// and its flag marks cell q, whose cubic spans nodes q - 1 .. q + 2.
+__global__ void __launch_bounds__(256) k_sigtab64(const SimConst<double> c, int e_lo, int blocks, int S,
+                                                   double* table) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= blocks * kSig64Rows) return;
+    const int blk = gid / kSig64Rows, q = gid % kSig64Rows;
+    const double base = ldexp(1.0, e_lo + blk), h = base / kSig64Cells;
+    const double E = base + (double)(q - 1) * h;
+    double* row = table + (size_t)gid * S;
+    const double invE = 1.0 / E;
+    double cum = sig_ruth<double>(c, E);
+    int col = 1;
+    row[col++] = E * cum;
+    cum += sig_moller<double>(c, E, invE);
+    row[col++] = E * cum;
+    for (int k = 0; k < c.nsh; ++k) {
+        cum += sig_gryz<double>(c, E, invE, k);
+        row[col++] = E * cum;
+    }
+    cum += sig_quinn<double>(c, E, invE);
+    row[0] = E * cum;
+    bool kink = false;
+    if (q < kSig64Cells) {
+        const double lo = E, hi = E + 3.0 * h;
+        auto in = [&](double x) { return x >= lo && x <= hi; };
+        kink = in(c.Wc) || in(c.Epl);
+        for (int k = 0; k < c.nsh; ++k) kink |= in(c.gEs[k]);
+    }
+    row[S - 1] = kink ? 1.0 : 0.0;
+}
+
 // Do two simulations have the same channel cross sections at every energy?
 // (material, Wc and density enter; beam, range and Bethe settings do not)
 inline bool same_sigma(const SimConst<double>& a, const SimConst<double>& b) {
@@ -487,15 +523,24 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
         // leave SMs idle, so that a small job spreads over the GPU: its
         // trajectories are latency chains, and an SM with fewer lanes runs
         // each chain faster (1000 FP32 electrons: 1.00 ms in 32 blocks of 32,
-        // 0.82 ms in 125 blocks of 8)
+        // 0.82 ms in 125 blocks of 8).  FP64 goes further, down to 2 threads
+        // while the grid stays within one warp per scheduler (4 per SM): an
+        // FP64 instruction occupies its scheduler's narrow FP64 unit for the
+        // whole warp however few lanes are active, so electrons spread over
+        // more schedulers finish sooner (1000 FP64 electrons with their
+        // table: 7.37 ms in blocks of 8, 6.69 ms in blocks of 2, 8.70 ms in
+        // blocks of 1, where schedulers hold two warps)
         block_size = 128;
         int dev = 0, sms = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return MCD_ECUDA;
         while (block_size > 8 && (sim->num_el + block_size - 1) / block_size < sms) block_size /= 2;
+        if (sim->precision == MCD_FP64)
+            while (block_size > 2 && 2 * ((sim->num_el + block_size - 1) / block_size) <= 4ll * sms) block_size /= 2;
     }
-    if (!(block_size == 8 || block_size == 16 || block_size % 32 == 0) || block_size > 256) return MCD_EINVAL;
+    if (!(block_size < 32 ? (block_size & (block_size - 1)) == 0 : block_size % 32 == 0) || block_size > 256)
+        return MCD_EINVAL;
     ElOut eo{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (electrons) {
         eo.outcome = electrons->outcome;
@@ -526,18 +571,30 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
 
 extern "C" size_t mcd_sigma_table_bytes(void) { return batch_sig_bytes(); }
 
-extern "C" int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat, float* table, void* stream) {
+extern "C" int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat, void* table, void* stream) {
     if (!sim || !mat || !table) return MCD_EINVAL;
     if (sim->mode != MCD_MODE_DS) return MCD_EINVAL;
+    if (sim->precision != MCD_FP32 && sim->precision != MCD_FP64) return MCD_EINVAL;
     if (sim->elastic < MCD_ELASTIC_RUTH || sim->elastic > MCD_ELASTIC_NIGRAM_WDEFL) return MCD_EINVAL;
     if (!(sim->E0 > sim->Emin) || !(sim->Emin > 0) || !(sim->Wc > 0)) return MCD_EINVAL;
     if (mat->n_shells < 0 || mat->n_shells > MCD_MAX_SHELLS || mat->atnd <= 0) return MCD_EINVAL;
     if ((reinterpret_cast<uintptr_t>(table) & 15) != 0) return MCD_EINVAL;   // rows are read as float4
+    if (sim->precision == MCD_FP64 && sigma_bytes64(sim->Emin, sim->E0, mat->n_shells + 3) > batch_sig_bytes())
+        return MCD_ETOOBIG;
     mcd_sim s = *sim;
     s.sigma_table = table;
-    const SimConst<double> c = make_consts<double>(s, *mat, nullptr, nullptr);
-    k_sigtab_one<<<(c.sig_rows + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        c, c.sig_l0, c.sig_inv, c.sig_rows, c.sig_S, table);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (sim->precision == MCD_FP64) {
+        const SimConst<double> c = make_consts<double>(s, *mat, nullptr, nullptr);
+        const int n = c.sig_rows * kSig64Rows;
+        k_sigtab64<<<(n + 255) / 256, 256, 0, st>>>(c, (int)c.sig_l0, c.sig_rows, c.sig_S,
+                                                     static_cast<double*>(table));
+        return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
+    }
+    s.precision = MCD_FP32;
+    SimConst<double> c = make_consts<double>(s, *mat, nullptr, nullptr);
+    k_sigtab_one<<<(c.sig_rows + 255) / 256, 256, 0, st>>>(c, c.sig_l0, c.sig_inv, c.sig_rows, c.sig_S,
+                                                            static_cast<float*>(table));
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 

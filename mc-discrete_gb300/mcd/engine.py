@@ -12,7 +12,7 @@ import numpy as np
 
 from . import _lib
 from .config import with_defaults
-from .tables import ds_tables, sigma_table
+from .tables import ds_tables, sigma_table, sigma_table_fits
 
 DEFAULT_HIST_E = (200, 100.0)   # 200 bins of 100 eV
 DEFAULT_HIST_T = (90, 1.0)      # 90 bins of 1 degree
@@ -105,11 +105,14 @@ def make_sim(input_par, num_el, seed=0, first_electron=0, precision=_lib.FP32, s
 
 
 def use_sigma_table(sim, mat, device="cuda"):
-    """Point a DS FP32 simulation at its cross-section table (built once per
-    parameter set and kept alive by the cache); returns the table, or None
-    when the simulation evaluates its cross sections inline (continuous mode,
-    FP64 transport)."""
-    if sim.mode != _lib.MODE_DS or sim.precision != _lib.FP32:
+    """Point a DS simulation at its cross-section table for its precision
+    (FP32: linear in log E; FP64: cubic on octave grids), built once per
+    parameter set and kept alive by the cache; returns the table, or None
+    when the simulation evaluates its cross sections inline (continuous
+    mode, or an FP64 energy range too wide for the table)."""
+    if sim.mode != _lib.MODE_DS:
+        return None
+    if sim.precision == _lib.FP64 and not sigma_table_fits(sim, mat):
         return None
     t = sigma_table(sim, mat, device)
     sim.sigma_table = t.data_ptr()
@@ -300,8 +303,8 @@ def run(input_par, num_el=None, seed=0, first_electron=0, precision="fp32", elec
         tally_channels=False, hist_E=DEFAULT_HIST_E, hist_T=DEFAULT_HIST_T, quirks=_lib.QUIRKS_REFERENCE,
         J_scale=1.0, n_scale=1.0, block_size=0, device="cuda", tables=None, ring_fields=0, tabulated=False):
     """Run one simulation to completion and return its results on the host.
-    tabulated: DS FP32 transport reads the channel cross sections from a
-    table (use_sigma_table) instead of evaluating them."""
+    tabulated: DS transport reads the channel cross sections from a table
+    for its precision (use_sigma_table) instead of evaluating them."""
     _torch()
     p = with_defaults(input_par)
     n = int(p["num_el"] if num_el is None else num_el)

@@ -261,14 +261,26 @@ def ds_tables(mat, E0, Emin, Wc, tol_E, tol_W, device="cuda"):
 _SIG_CACHE = {}
 
 
+SIG64_CELLS, SIG64_ROWS = 256, 259
+
+
+def sigma_table_fits(sim, mat):
+    """Does the FP64 table of this simulation's energy range fit the buffer
+    (mcd_sigma_table_bytes)?  One block of 259 rows of n_shells + 4 doubles
+    per octave of (Emin, E0]."""
+    octaves = math.frexp(float(sim.E0))[1] - math.frexp(float(sim.Emin))[1] + 1
+    return 8 * octaves * SIG64_ROWS * (mat.n_shells + 4) <= _lib.lib().mcd_sigma_table_bytes()
+
+
 def sigma_table(sim, mat, device="cuda"):
-    """Device cross-section table of a DS simulation (mcd_build_sigma_table:
-    E times the total and running channel cross sections on a log2-E grid
-    over [Emin, E0]), cached per material, Wc, elastic model, density scale
-    and energy range."""
+    """Device cross-section table of a DS simulation for its precision
+    (mcd_build_sigma_table: E times the total and running channel cross
+    sections over [Emin, E0]; FP32 on a log2-E grid, FP64 on octave grids),
+    cached per material, Wc, elastic model, density scale, energy range and
+    precision."""
     import torch
     key = (bytes(mat), int(sim.elastic), float(sim.Wc), float(sim.n_scale), float(sim.E0), float(sim.Emin),
-           str(device))
+           int(sim.precision), str(device))
     t = _SIG_CACHE.get(key)
     if t is None:
         t = torch.empty(_lib.lib().mcd_sigma_table_bytes() // 4, dtype=torch.float32, device=device)

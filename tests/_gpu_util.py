@@ -41,9 +41,10 @@ def host_copies(dev_tables):
     return out
 
 
-def run_pair(p, n, seed=1, precision="fp64", nthreads=None):
-    """GPU run and C-oracle run of the same n electrons."""
-    g = engine.run(p, num_el=n, seed=seed, precision=precision)
+def run_pair(p, n, seed=1, precision="fp64", nthreads=None, tabulated=False):
+    """GPU run and C-oracle run of the same n electrons (tabulated: the GPU
+    reads the simulation's cross-section table for its precision)."""
+    g = engine.run(p, num_el=n, seed=seed, precision=precision, tabulated=tabulated)
     mat = O.Material(p["material"])
     ds = "DS" in p["mode"]
     ht = host_copies(gpu_tables(p)) if ds else None

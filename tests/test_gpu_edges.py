@@ -122,14 +122,14 @@ def test_electron_indices_above_two_to_the_32():
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
 def test_block_size_does_not_change_results(prec):
-    """Blocks of 8 and 16 threads (what a small job gets automatically) give
+    """Blocks of 1 to 16 threads (what a small job gets automatically) give
     the trajectories of full-warp blocks; other sizes are rejected."""
-    runs = [engine.run(SI, num_el=300, seed=4, precision=prec, block_size=b) for b in (8, 16, 32, 128, 0)]
+    runs = [engine.run(SI, num_el=300, seed=4, precision=prec, block_size=b) for b in (8, 1, 2, 4, 16, 32, 128, 0)]
     for g in runs[1:]:
         for k in INT_KEYS:
             assert g.tally[k] == runs[0].tally[k], k
         assert np.array_equal(g.electrons["n_events"], runs[0].electrons["n_events"])
         assert np.array_equal(g.electrons["final_E"], runs[0].electrons["final_E"])
-    for b in (4, 24, 48, 512):
+    for b in (3, 24, 48, 512):
         with pytest.raises(_lib.MCDError):
             engine.run(SI, num_el=10, seed=4, precision=prec, block_size=b)

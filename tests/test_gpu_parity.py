@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 from scipy import stats
 
+from mcd import engine
 from _gpu_util import eta_z, input_par, run_pair
 
 pytestmark = pytest.mark.gpu
@@ -53,6 +54,40 @@ def test_fp64_follows_oracle_trajectories(name, p, n):
     if p.get("diffMFP"):
         assert t["trdf"] == int((e["outcome"] == 4).sum()) > 0
         assert abs(t["trdf"] - int((c["outcome"] == 4).sum())) <= 0.01 * n
+
+
+DS_CASES = [c for c in CASES if "_ds" in c[0] or c[0] == "si_film_diff"]
+
+
+@pytest.mark.parametrize("name,p,n", DS_CASES, ids=[c[0] for c in DS_CASES])
+def test_fp64_tabulated_follows_oracle_trajectories(name, p, n):
+    """FP64 transport reading its FP64 cross-section table (cubic on octave
+    grids, within about 4e-10 of the exact sums; exact where a channel
+    threshold lies in the cell) follows the oracle like the inline path:
+    a channel decision moves only when a draw falls that close to a
+    boundary."""
+    g, c = run_pair(p, n, seed=123, precision="fp64", tabulated=True)
+    e = g.electrons
+    same = (e["outcome"] == c["outcome"]) & (e["n_events"] == c["n_events"])
+    assert same.mean() >= 0.99, (name, same.mean())
+    fe_ok = np.abs(e["final_E"] - c["final_E"]) <= 1e-9 * np.abs(c["final_E"])
+    assert (same & fe_ok).mean() >= 0.99, name
+    d_ok = np.abs(e["dir"] - c["dir"]).max(axis=1) <= 1e-9
+    d_ok |= np.isnan(c["dir"]).any(axis=1) & np.isnan(e["dir"]).any(axis=1)
+    assert (same & d_ok).mean() >= 0.99, name
+    assert g.tally["bks"] + g.tally["abs"] + g.tally["trsm"] + g.tally["trdf"] + g.tally["long"] == n
+
+
+def test_fp64_table_equals_inline_on_the_small_configuration():
+    """The small FP64 configuration (Si 10 keV, 1000 electrons): with the
+    table every trajectory matches the inline run's."""
+    p = input_par("Si", 10000.0, 1000.0, 0.0)
+    a = engine.run(p, num_el=1000, seed=0, precision="fp64")
+    b = engine.run(p, num_el=1000, seed=0, precision="fp64", tabulated=True)
+    ea, eb = a.electrons, b.electrons
+    same = (ea["outcome"] == eb["outcome"]) & (ea["n_events"] == eb["n_events"])
+    assert same.mean() >= 0.999, same.mean()
+    assert np.all(np.abs(ea["final_E"][same] - eb["final_E"][same]) <= 1e-9 * np.abs(ea["final_E"][same]))
 
 
 @pytest.mark.parametrize("name,p,n", CASES, ids=[c[0] for c in CASES])

@@ -199,6 +199,16 @@ def test_new_fields_are_validated_before_any_gpu_work():
     assert L.mcd_run(C.byref(s), C.byref(mat), None, None, 1, None, None, 1, 128, None) == _lib.EINVAL
     assert L.mcd_build_sigma_table(C.byref(s), C.byref(mat), None, None) == _lib.EINVAL
     assert L.mcd_sigma_table_bytes() == 4 * 4096 * 12
+    # an FP64 table covers whole octaves of (Emin, E0]: 100 eV to 30 keV for
+    # Au (nine octaves of 259 rows x 12 doubles) exceeds the buffer; the
+    # size is checked before any launch
+    au = _lib.material("Au")
+    s = engine.make_sim(dict(material="Au", E0=30000.0, Emin=100.0, Wc=50.0, mode="DS"), 16, precision=_lib.FP64)
+    tbl = (C.c_double * 4)()
+    addr = (C.addressof(tbl) + 15) & ~15            # 16-byte aligned, as the entry point requires
+    assert L.mcd_build_sigma_table(C.byref(s), C.byref(au), C.c_void_p(addr), None) == _lib.ETOOBIG
+    s.sigma_table = addr
+    assert L.mcd_run(C.byref(s), C.byref(au), None, None, 1, None, None, 1, 128, None) == _lib.ETOOBIG
     # the reserved tuning word must be zero (host buffers: nothing is dereferenced)
     host = (C.c_uint8 * 64)()
     t = _lib.Tune(256, 0, 1, 0, 5)
