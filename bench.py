@@ -208,8 +208,11 @@ CFG1_WORKLOAD = ("DS Si, E0 10 keV, Emin 1 keV, tilt 0 deg, Wc 100 eV, tol 1e-3,
 
 def cfg1_bench(args, dev):
     """The small plain configuration in full on both sides: one FP64 launch
-    against the C oracle on 1 core and on all host cores (same Philox stream,
-    so the two follow the same trajectories)."""
+    (automatic block size) against the C oracle on 1 core and on all host
+    cores (same Philox stream, so the two follow the same trajectories).
+    The GPU reads the simulation's FP64 cross-section table (cubic on octave
+    grids); the launch that evaluates every cross section per event is timed
+    beside it, and the FP32 launch with its FP32 table."""
     import torch
     import coracle
     import mcd_oracle as O
@@ -218,53 +221,56 @@ def cfg1_bench(args, dev):
     n = 1000
     mat = _lib.material("Si")
     dt = tables.ds_tables(mat, 10000.0, 1000.0, 100.0, 1e-3, 1e-3, dev)
-    sim = engine.make_sim(p, n, seed=args.seed, precision=_lib.FP64)
-    bufs = engine.RunBuffers(n, _lib.FP64, True, 0, device=dev)
     stream = torch.cuda.current_stream(dev)
-    for _ in range(args.warmup):
-        bufs.zero()
-        engine.launch(sim, mat, dt, bufs)
-    torch.cuda.synchronize(dev)
-    ms = []
-    for _ in range(max(3, args.steps)):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        bufs.zero()
-        e0.record(stream)
-        engine.launch(sim, mat, dt, bufs)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms.append(e0.elapsed_time(e1))
-    g = engine.collect(bufs)
-    # the same launch in FP32 transport, with the simulation's cross-section table
+
+    def timed(sim, prec):
+        bufs = engine.RunBuffers(n, prec, True, 0, device=dev)
+        ms = []
+        for k in range(args.warmup + max(3, args.steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            bufs.zero()
+            e0.record(stream)
+            engine.launch(sim, mat, dt, bufs)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            if k >= args.warmup:
+                ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms), engine.collect(bufs)
+
+    sim = engine.make_sim(p, n, seed=args.seed, precision=_lib.FP64)
+    engine.use_sigma_table(sim, mat, dev)
+    ms, g = timed(sim, _lib.FP64)
+    ms_inline, gi = timed(engine.make_sim(p, n, seed=args.seed, precision=_lib.FP64), _lib.FP64)
     sim32 = engine.make_sim(p, n, seed=args.seed, precision=_lib.FP32)
     engine.use_sigma_table(sim32, mat, dev)
-    b32 = engine.RunBuffers(n, _lib.FP32, True, 0, device=dev)
-    ms32 = []
-    for k in range(args.warmup + max(3, args.steps)):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        b32.zero()
-        e0.record(stream)
-        engine.launch(sim32, mat, dt, b32)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        if k >= args.warmup:
-            ms32.append(e0.elapsed_time(e1))
+    ms32, _ = timed(sim32, _lib.FP32)
     om = O.Material("Si")
     ht = [coracle.HostTable(t.Ws.cpu().numpy(), t.Es.cpu().numpy(), t.cdf.cpu().numpy()) for t in dt]
     cpu = {}
     for th in (1, os.cpu_count() or 1):
-        t0 = time.perf_counter()
-        c = coracle.run(om, 10000.0, 1000.0, 0.0, n, seed=args.seed, mode="DS", Wc=100.0, tables=ht, nthreads=th)
-        cpu[th] = time.perf_counter() - t0
+        best = float("inf")
+        for _ in range(3 if th > 1 else 1):
+            t0 = time.perf_counter()
+            c = coracle.run(om, 10000.0, 1000.0, 0.0, n, seed=args.seed, mode="DS", Wc=100.0, tables=ht, nthreads=th)
+            best = min(best, time.perf_counter() - t0)
+        cpu[th] = best
     ev = int(g.tally["events"])
-    same = float(np.mean((g.electrons["outcome"] == c["outcome"]) & (g.electrons["n_events"] == c["n_events"])))
-    return {"workload": CFG1_WORKLOAD, "num_el": n, "events": ev, "gpu_ms": statistics.median(ms),
-            "gpu_events_per_s": ev / statistics.median(ms) * 1e3, "gpu_fp32_ms": statistics.median(ms32),
-            "note": "1000 electrons make 125 blocks of 8 threads: the launch lasts as long as its longest "
-                    "trajectory, and FP64 arithmetic runs at a small fraction of the FP32 rate on this GPU",
+
+    def same(r):
+        return float(np.mean((r.electrons["outcome"] == c["outcome"]) & (r.electrons["n_events"] == c["n_events"])))
+
+    return {"workload": CFG1_WORKLOAD, "num_el": n, "events": ev, "gpu_ms": ms, "gpu_events_per_s": ev / ms * 1e3,
+            "cross_sections": "FP64 table, cubic on octave grids (exact in cells that straddle a threshold)",
+            "gpu_inline_ms": ms_inline, "gpu_fp32_ms": ms32,
+            "longest_electron_events": int(g.electrons["n_events"].max()),
+            "note": "the launch lasts as long as its longest trajectory; every FP64 instruction occupies its "
+                    "scheduler's narrow FP64 unit for the whole warp, so the automatic block size spreads "
+                    "the electrons over the schedulers (blocks of 2)",
             "cpu_1core_s": cpu[1], "cpu_all_cores_s": cpu[os.cpu_count() or 1], "cpu_cores": os.cpu_count() or 1,
+            "cpu_timing": "best of 3 on all cores, one run on 1 core",
             "eta_gpu_fp64": g.tally["bks"] / n, "eta_oracle": float(np.mean(c["outcome"] == 1)),
-            "identical_trajectories": same, "gpu_launches": 2 * max(3, args.steps)}
+            "identical_trajectories": same(g), "identical_trajectories_inline": same(gi),
+            "gpu_launches": 3 * (args.warmup + max(3, args.steps))}
 
 
 def bench_config(sims):
@@ -361,11 +367,23 @@ def adjoint_bench(args, dev):
     Lm = float(np.sum((m.chain(1 - d, 1.0)[0] - t) ** 2))
     fd = (Lp - Lm) / (2 * d)
     h, _, _ = m.forward(1.0, 1.0)     # restore the checkpoints of J = 1
+    # the re-simulated central difference with common random numbers
+    # (every electron free to change its event sequence), split into the
+    # electrons whose exit event stayed and the jump part of the others
+    from mcd.adjoint import resimulated_fd
+    r = resimulated_fd(m, t, h=d)
+    crn = {"dL_dJscale": r["fd"], "rel_err": abs(dJ - r["fd"]) / abs(r["fd"]),
+           "z": (r["fd"] - dJ) / r["jump_se"], "same_sequence_dL_dJscale": r["fd_same_sequence"],
+           "same_sequence_rel_err": abs(dJ - r["fd_same_sequence"]) / abs(dJ), "jump_part": r["fd_jump"],
+           "jump_se_rel": r["jump_se"] / abs(dJ), "electrons_changed": r["changed"],
+           "note": "the jump part is noise of standard error ~ 1/sqrt(N h) (16 seeds: mean 1.3% +- 2.9% of the "
+                   "gradient), so agreement is judged by z = (FD - adjoint) / its standard error"}
     depth = adjoint_depth_bench(args, dev, p, n)
     return {"workload": ADJ_WORKLOAD, "num_el": n, "fwd_ms": tf / args.steps, "bwd_ms": tb / args.steps,
             "bwd_over_fwd": tb / tf, "loss": L, "dL_dJscale": dJ, "dL_dnscale": dn,
             "fd_frozen_dL_dJscale": fd, "fd_frozen_rel_err": abs(dJ - fd) / abs(fd) if fd else None,
-            "fd_step": d, "max_depth": depth, "gpu_launches": 2 * args.steps + depth["gpu_launches"]}
+            "fd_crn": crn, "fd_crn_rel_err": crn["rel_err"],
+            "fd_step": d, "max_depth": depth, "gpu_launches": 2 * args.steps + depth["gpu_launches"] + 3}
 
 
 def adjoint_depth_bench(args, dev, p, n):

@@ -6,13 +6,14 @@ The adjoint gives the pathwise derivative with the random numbers and the
 event sequence frozen; it is checked against central finite differences of
 exactly that function (the exit energies recomputed along the frozen event
 sequence, mcd_adjoint_chain), in FP64 and in FP32, and against the FP64
-adjoint.  The full re-simulated finite difference (common random numbers,
-event sequence free to change) is reported alongside."""
+adjoint.  The re-simulated finite difference (common random numbers, event
+sequence free to change) is split into the electrons whose exit event
+stayed the same and the jump part of those whose exit event changed."""
 import numpy as np
 import pytest
 import torch
 
-from mcd.adjoint import ExitEnergyModel, exit_histogram
+from mcd.adjoint import ExitEnergyModel, exit_histogram, resimulated_fd
 from _gpu_util import input_par
 
 pytestmark = pytest.mark.gpu
@@ -71,17 +72,31 @@ def test_fp32_adjoint_against_fd_and_fp64():
 
 
 def test_full_resimulation_fd_is_close():
-    """Re-simulating at J(1 +- d) also moves a few exit events; the pathwise
-    derivative ignores those, so agreement is loose (reported, not exact)."""
-    m = ExitEnergyModel(AL, 50000, seed=7, precision="fp64")
+    """The finite difference of the benchmark spec's check: central, relative
+    step 1e-3, common random numbers, every electron re-simulated at
+    J (1 +- 1e-3), at the size of the differentiable workload (Al 15 keV,
+    70 deg, 1e6 electrons, FP32).  Re-simulation lets about 0.35% of the
+    electrons change their exit event; their soft-bin terms jump, so the
+    difference is the pathwise derivative plus a jump part whose standard
+    error (from its independent per-electron terms) is about 10% of the
+    gradient at this size, shrinking as 1/sqrt(N h).  Over 16 seeds the jump
+    part averaged 1.3% +- 2.9% of the gradient: no bias the pathwise
+    estimator misses.  So the checks are
+      * the electrons whose exit event stayed the same: their difference
+        equals the adjoint within 2% (0.05-1.6% over 16 seeds; the rest is
+        the pathwise terms of the electrons that changed, which this part
+        leaves out, and it falls as 1/sqrt(N): 0.01-0.3% at 4e6);
+      * the whole difference: within 4 standard errors of its jump part."""
+    m = ExitEnergyModel(AL, 1000000, seed=7, precision="fp32")
     t, _, _ = m.forward(1.1, 1.0)
     _, dJ, _ = loss_grad(m, t)
-    d = 1e-3
-    Lp = float(np.sum((m.forward(1 + d, 1.0)[0] - t) ** 2))
-    Lm = float(np.sum((m.forward(1 - d, 1.0)[0] - t) ** 2))
-    fd = (Lp - Lm) / (2 * d)
-    assert np.sign(fd) == np.sign(dJ)
-    assert abs(dJ - fd) <= 0.3 * abs(fd), (dJ, fd)
+    r = resimulated_fd(m, t, h=1e-3)
+    assert np.sign(r["fd_same_sequence"]) == np.sign(dJ)
+    assert abs(dJ - r["fd_same_sequence"]) <= 2e-2 * abs(dJ), (dJ, r)
+    assert abs(r["fd"] - dJ) <= 4.0 * r["jump_se"], (dJ, r)
+    assert 0.001 < r["changed"] / 1e6 < 0.01, r
+    # the split is exact: the two parts add up to the difference of the losses
+    assert abs(r["fd_jump"] + r["fd_same_sequence"] - r["fd"]) <= 1e-6 * abs(r["fd"]) + 1e-15
 
 
 def test_autograd_function_matches_model():
