@@ -588,7 +588,10 @@ def detector_bench(args, dev):
         torch.cuda.synchronize(dev)
         times.append(e0.elapsed_time(e1) * 1e-3)
     t = statistics.median(times)
-    peak = float(measured_peaks().get("hbm_gbs", 6800.0))
+    pk = measured_peaks()
+    peak = float(pk.get("hbm_gbs", 6800.0))
+    peak_note = ("measured copy bandwidth (MEASURED_PEAKS.json)" if "hbm_gbs" in pk else
+                 "fallback 6.8 TB/s: no measured-peaks file on this host")
     gbs = 20.0 * n / t / 1e9
     cpu = None
     if not args.no_cpu:
@@ -605,7 +608,7 @@ def detector_bench(args, dev):
                "max_abs_err_um": float(err.max()), "max_rel_err": float((err / np.maximum(np.abs(ref), 1.0)).max())}
     return {"workload": DET_WORKLOAD, "n": n, "ms": t * 1e3, "directions_per_s": n / t,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                         "bytes_per_direction": 20, "peak_note": "measured copy bandwidth"},
+                         "bytes_per_direction": 20, "peak_note": peak_note},
             "cpu_baseline": cpu, "gpu_launches": max(3, args.steps)}
 
 
