@@ -51,14 +51,14 @@ CPU_SAMPLE_ELECTRONS = 40000
 # the figure does not grow with the electrons)
 BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
 # warp instructions issued per event by the batched kernel on this workload,
-# from an ncu capture of a quarter-size launch (2.030e10 instructions for
+# from an ncu capture of a quarter-size launch (2.0172e10 instructions for
 # 1.3855e9 events); the issue peak is one warp instruction per scheduler
 # per cycle, 4 schedulers per SM
-WARP_INST_PER_EVENT = 14.65
+WARP_INST_PER_EVENT = 14.56
 # the same capture's unit fractions (of peak sustained): issue-active cycles,
 # threads per warp instruction / 32, the L1/TEX unit, its shared-memory
 # wavefronts, and L2
-BATCHED_NCU = {"issue_active": 0.765, "warp_execution_efficiency": 0.711, "l1tex_throughput": 0.711,
+BATCHED_NCU = {"issue_active": 0.765, "warp_execution_efficiency": 0.709, "l1tex_throughput": 0.723,
                "shared_wavefronts": 0.284, "l2_throughput": 0.018,
                "capture": "ncu --set full of k_batched on a quarter of the workload (1.3855e9 events)"}
 
@@ -936,8 +936,17 @@ def main():
     ap.add_argument("--no-tables", action="store_true", help="skip the table-build timing")
     ap.add_argument("--stream-fraction", type=float, default=1.0,
                     help="fraction of the 1e7-electron streaming workload to run (1 = all of it)")
+    ap.add_argument("--section", default="", choices=("", "cfg1", "cont", "adjoint", "stream", "detector", "tables"),
+                    help="run one section alone on cuda:0 and print its JSON (for profiling); not the bench line")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.section:
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        fn = {"cfg1": cfg1_bench, "cont": cont_bench, "adjoint": adjoint_bench, "stream": stream_bench,
+              "detector": detector_bench, "tables": tables_bench}[args.section]
+        print(json.dumps({args.section: fn(args, dev)}), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_mcd(args)
