@@ -767,14 +767,7 @@ def run_mcd(args):
     def summed(tl):
         """Tallies summed over the ranks (each rank transported its own
         electrons): one collective of the integer counts, one of the FP64 sums."""
-        if dist is None:
-            return tl
-        v = torch.from_numpy(np.stack([shard.tally_vector(t) for t in tl])).to(dev)
-        s = torch.tensor([[t[k] for k in shard.SUM_KEYS] for t in tl], dtype=torch.float64, device=dev)
-        dist.all_reduce(v)
-        dist.all_reduce(s)
-        return [shard.tally_from_vector(a, dict(zip(shard.SUM_KEYS, b)))
-                for a, b in zip(v.cpu().numpy(), s.cpu().numpy())]
+        return tl if dist is None else shard.allreduce_tallies(tl, dist, dev)
 
     tallies, ptallies, pitallies = summed(tallies), summed(ptallies), summed(pitallies)
     if dist is not None:

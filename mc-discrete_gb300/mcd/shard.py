@@ -57,3 +57,18 @@ def tally_from_vector(v, sums=None):
     for k in SUM_KEYS:
         out[k] = float(sums[k]) if sums else 0.0
     return out
+
+
+def allreduce_tallies(tallies, dist, device=None):
+    """The per-simulation tallies of this rank summed over every rank of the
+    default process group (torch.distributed): one all-reduce of the integer
+    counts (tally_vector) and one of the FP64 sums, on `device` (the rank's
+    GPU under NCCL; None keeps them on the host, as gloo wants)."""
+    import torch
+    v = torch.from_numpy(np.stack([tally_vector(t) for t in tallies]).astype(np.int64))
+    s = torch.tensor([[float(t[k]) for k in SUM_KEYS] for t in tallies], dtype=torch.float64)
+    if device is not None:
+        v, s = v.to(device), s.to(device)
+    dist.all_reduce(v)
+    dist.all_reduce(s)
+    return [tally_from_vector(a, dict(zip(SUM_KEYS, b))) for a, b in zip(v.cpu().numpy(), s.cpu().numpy())]

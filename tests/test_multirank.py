@@ -66,6 +66,41 @@ def _worker(rank, world, port, n, out_path):
     dist.destroy_process_group()
 
 
+def _tally(seed):
+    rng = np.random.default_rng(seed)
+    t = {k: int(rng.integers(0, 1000)) for k in shard.INT_KEYS}
+    t.update({k: float(rng.uniform(0, 1e6)) for k in shard.SUM_KEYS})
+    t.update(channel=rng.integers(0, 100, 16), hist_E=rng.integers(0, 100, 256), hist_T=rng.integers(0, 100, 180))
+    return t
+
+
+def _allreduce_worker(rank, world, port, out_path):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    got = shard.allreduce_tallies([_tally(10 * rank + k) for k in range(3)], dist)
+    if rank == 0:
+        np.save(out_path, np.array([np.concatenate([shard.tally_vector(t), [t[k] for k in shard.SUM_KEYS]])
+                                    for t in got], dtype=np.float64))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_allreduce_tallies_sums_every_simulation(tmp_path):
+    """The bench's whole-job counts under torchrun: every simulation's tally
+    summed over two gloo ranks equals the host-side merge of the ranks'
+    tallies."""
+    out = str(tmp_path / "sums.npy")
+    tmp.start_processes(_allreduce_worker, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    got = np.load(out)
+    for k in range(3):
+        m = shard.merge_tallies([_tally(k), _tally(10 + k)])
+        want = np.concatenate([shard.tally_vector(m), [m[key] for key in shard.SUM_KEYS]])
+        assert np.array_equal(got[k][:-3], want[:-3]), k
+        assert np.allclose(got[k][-3:], want[-3:], rtol=1e-15), k
+
+
 def test_shard_ranges_cover_exactly():
     n = 1001
     got = [shard.shard_range(n, 3, r, first=7) for r in range(3)]
