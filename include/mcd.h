@@ -246,7 +246,8 @@ typedef struct mcd_tune {
     int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid */
     int32_t refill;          /* idle lanes a warp waits for before it takes
                                 new electrons from the queue (1..32)          */
-    int32_t variant;         /* bit 0: 48-register kernel (block_size <= 256)
+    int32_t variant;         /* bit 0: 56-register kernel (block_size <= 576,
+                                two blocks per SM)
                                 instead of the 64-register one; bit 1: evaluate
                                 cross sections inline instead of from the
                                 tables mcd_batch_prepare builds              */
@@ -417,7 +418,7 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * packed on the host and handed to a staging kernel on `stream` as one
  * kernel argument, so no host memory has to outlive the call;
  * tallies[nsims] (zeroed by the caller) and status are device pointers.
- * tune is read as by mcd_run_batched (variant bit 0: the 48-register
+ * tune is read as by mcd_run_batched (variant bit 0: the 56-register
  * kernel; bit 1: inline cross sections).  Without bit 1 a simulation that
  * carries a caller-built sigma_table reads it; the others evaluate their
  * cross sections inline (there is no room for tables in the array).       */

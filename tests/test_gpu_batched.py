@@ -165,8 +165,17 @@ def test_autotune_picks_a_measured_shape(tmp_path, monkeypatch):
     k = "%d/%d/%d" % (t.block_size, t.refill, t.variant)
     full = {key[5:]: ms for key, ms in table.items() if key.startswith("full:")}
     scaled = {key: ms for key, ms in table.items() if not key.startswith("full:")}
-    # the finalists are the three fastest on the scaled copy; the batch itself decides
-    assert set(full) == set(sorted(scaled, key=scaled.get)[:3])
+    # the finalists are the three fastest on the scaled copy and, for every
+    # (block, register budget) pair, its fastest refill and refill 1; the
+    # batch itself decides
+    want = set(sorted(scaled, key=scaled.get)[:3])
+    for b_ in (128, 256):
+        for v in (0, 1):
+            of = [key for key in scaled if key.startswith("%d/" % b_) and key.endswith("/%d" % v)]
+            if of:
+                want.add(min(of, key=scaled.get))
+                want |= {key for key in of if key.split("/")[1] == "1"}
+    assert set(full) == want
     assert k in full and min(full.values()) == full[k]
     t2, _ = autotune.tune(b)          # from the cache
     assert (t2.block_size, t2.refill) == (t.block_size, t.refill)

@@ -82,7 +82,7 @@ def test_noalloc_reads_caller_built_cross_section_tables():
 
 def test_noalloc_honours_the_tune_variant_bits():
     """Bit 1 evaluates the cross sections inline even for simulations that
-    carry a caller-built table; bit 0 runs the 48-register kernel.  Both
+    carry a caller-built table; bit 0 runs the 56-register kernel.  Both
     give the workspace run's tallies under the same bits."""
     b = engine.Batch(SIMS, seed=23)
     keep = [engine.use_sigma_table(b._sims_arr[k], b.mats[b._idx[0][k]]) for k in range(b.n)]
@@ -94,7 +94,7 @@ def test_noalloc_honours_the_tune_variant_bits():
         _same(got, ref)
         assert st == st_ref
     with pytest.raises(_lib.MCDError):
-        _noalloc(b, _lib.Tune(512, 0, 1, 1, 0))     # the 48-register kernel takes at most 256 threads
+        _noalloc(b, _lib.Tune(640, 0, 1, 1, 0))     # the 56-register kernel takes at most 576 threads
 
 
 def test_noalloc_at_its_limit_of_64_simulations():
