@@ -2,7 +2,8 @@
 the batched benchmark ({Al,Si,Cu,Au} x E0 {5,10,20,30} keV x tilt
 {0,20,45,70} deg, Emin 1 keV, Wc 100 eV, tol 1e-3) at min(num_el, 2000)
 electrons, run as one persistent launch in the configuration the benchmark
-times (tabulated cross sections, block 1024, refill 1), against the FP64
+times (tabulated cross sections, two blocks of 576 per SM at 56 registers,
+refill 1), against the FP64
 C oracle on its own tables (the reference's W/E grids from
 tests/golden/tables.npz) and an independent Philox seed:
   * eta of every simulation within 3 sigma, Bonferroni-adjusted over the 64
