@@ -307,7 +307,9 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
     uint32_t st = 0;
     const mcd_electron_out* rows = reinterpret_cast<const mcd_electron_out*>(ws + batch_elout_off(nsims));
     while (true) {
-        const unsigned idle = __ballot_sync(0xffffffffu, !have);
+        // the lanes without an electron; voted again only after a refill,
+        // so a step with every lane busy costs one vote
+        unsigned idle = __ballot_sync(0xffffffffu, !have);
         if (!exhausted && idle && (__popc(idle) >= refill || idle == 0xffffffffu)) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(&hdr->queue, (unsigned long long)__popc(idle));
@@ -327,8 +329,9 @@ __device__ __forceinline__ void batched_body(uint8_t* ws, mcd_tally* tallies, in
                 }
             }
             if (base + __popc(idle) >= total) exhausted = true;
+            idle = __ballot_sync(0xffffffffu, !have);
         }
-        if (!__any_sync(0xffffffffu, have)) {
+        if (idle == 0xffffffffu) {
             if (exhausted) break;
             continue;
         }
