@@ -50,17 +50,19 @@ CPU_SAMPLE_ELECTRONS = 40000
 # from an ncu capture of that launch (tables and workspace read about once;
 # the figure does not grow with the electrons)
 BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
-# warp instructions issued per event by the batched kernel on this workload,
-# from an ncu capture of a quarter-size launch (2.0172e10 instructions for
-# 1.3855e9 events); the issue peak is one warp instruction per scheduler
-# per cycle, 4 schedulers per SM
-WARP_INST_PER_EVENT = 14.56
+# warp instructions issued per event by the batched kernel on this workload
+# in its tuned shape (two blocks of 576 per SM, 56 registers), from an ncu
+# capture of a quarter-size launch (2.0314e10 instructions for 1.3855e9
+# events); the issue peak is one warp instruction per scheduler per cycle,
+# 4 schedulers per SM
+WARP_INST_PER_EVENT = 14.66
 # the same capture's unit fractions (of peak sustained): issue-active cycles,
 # threads per warp instruction / 32, the L1/TEX unit, its shared-memory
 # wavefronts, and L2
-BATCHED_NCU = {"issue_active": 0.765, "warp_execution_efficiency": 0.709, "l1tex_throughput": 0.723,
-               "shared_wavefronts": 0.284, "l2_throughput": 0.018,
-               "capture": "ncu --set full of k_batched on a quarter of the workload (1.3855e9 events)"}
+BATCHED_NCU = {"issue_active": 0.776, "warp_execution_efficiency": 0.706, "l1tex_throughput": 0.738,
+               "shared_wavefronts": 0.293, "l2_throughput": 0.029,
+               "capture": "ncu --set full of k_batched_lr (2 x 576, 56 registers) on a quarter of the workload "
+                          "(1.3855e9 events)"}
 
 
 def workload(scale=1.0):
