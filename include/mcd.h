@@ -109,7 +109,9 @@ typedef struct mcd_table {
     const float* Es;         /* device, nE energies (float32 linspace)        */
     const float* Ws;         /* device, nW energy losses (float32 geomspace)  */
     const float* cdf;        /* device, nE x (nW-1); 0 marks a masked entry   */
-    const int32_t* nvalid;   /* device, nE unmasked counts per row, or NULL   */
+    const int32_t* nvalid;   /* device, nE unmasked counts per row, or NULL
+                                (written by mcd_build_table; the transport
+                                does not read it: masked entries act as +inf) */
     const uint16_t* guide;   /* device, nE x (MCD_GUIDE+1): first CDF index
                                 whose value is >= k/MCD_GUIDE, or NULL (needs
                                 nW - 1 <= 65535); a draw U lies between entries

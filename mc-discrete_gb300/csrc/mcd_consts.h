@@ -50,7 +50,8 @@ struct TableDev {
     const float* Es;
     const float* Ws;
     const float* cdf;
-    const int32_t* nvalid;
+    float inv_dE;      // (nE - 1) / (E_last - E_first), 0 if unknown
+    int32_t reserved_;
     const uint16_t* guide;
     int32_t nE;
     int32_t nW;
@@ -258,9 +259,15 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
     c.hT = s.hist_T_bins;
     c.invWE = (T)(s.hist_E_width > 0 ? 1.0 / s.hist_E_width : 0.0);
     c.invWT = (T)(s.hist_T_width > 0 ? 1.0 / s.hist_T_width : 0.0);
-    TableDev z{nullptr, nullptr, nullptr, nullptr, nullptr, 0, 0, 0.0f, 0.0f};
-    c.tab[0] = tm ? TableDev{tm->Es, tm->Ws, tm->cdf, tm->nvalid, tm->guide, tm->nE, tm->nW, tm->E_first, tm->E_last} : z;
-    c.tab[1] = tg ? TableDev{tg->Es, tg->Ws, tg->cdf, tg->nvalid, tg->guide, tg->nE, tg->nW, tg->E_first, tg->E_last} : z;
+    TableDev z{nullptr, nullptr, nullptr, 0.0f, 0, nullptr, 0, 0, 0.0f, 0.0f};
+    auto td = [](const mcd_table* t) {
+        TableDev d{t->Es, t->Ws, t->cdf, 0.0f, 0, t->guide, t->nE, t->nW, t->E_first, t->E_last};
+        if (t->E_last > t->E_first && t->nE > 1)
+            d.inv_dE = (float)((double)(t->nE - 1) / ((double)t->E_last - (double)t->E_first));
+        return d;
+    };
+    c.tab[0] = tm ? td(tm) : z;
+    c.tab[1] = tg ? td(tg) : z;
     // the caller's table (mcd_run), or none until a batch shares one among
     // the simulations it fits
     c.sig = nullptr;

@@ -149,7 +149,7 @@ __device__ __forceinline__ int table_row(const TableDev& t, T E, bool* out_of_ra
     if (!(E > (T)e0)) return 0;
     // linear-grid guess, then an exact correction against the stored values
     // (computed in T: a guess only, the search below corrects it exactly)
-    int g = (int)ceil((E - (T)e0) * (T)(nE - 1) / (T)(eL - e0));
+    int g = (int)ceil((E - (T)e0) * (t.inv_dE > 0.0f ? (T)t.inv_dE : (T)(nE - 1) / (T)(eL - e0)));
     g = g < 1 ? 1 : (g > nE - 1 ? nE - 1 : g);
     int lo = 0, hi = nE - 1;  // invariant: Es[lo] < E <= Es[hi]
     {
@@ -171,11 +171,14 @@ __device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) 
     const int kq = (int)(U * (T)MCD_GUIDE);
     int i = -1, lo = 0, hi = 0;
     if (t.guide && t.E_last > 0.0f && E > (T)t.E_first && !(E > (T)t.E_last)) {
-        // the row guess's bracketing energies and its guide entries in one
-        // round trip, kept when the guess is the row (as it usually is: the
-        // E grid is a float32 linspace); otherwise the search below
+        // the row guess (from the table's inverse grid step, no division),
+        // its bracketing energies and its guide entries in one round trip,
+        // kept when the guess is the row (as it usually is: the E grid is a
+        // float32 linspace); otherwise the search below
         const int nE = t.nE;
-        int g = (int)ceil((E - (T)t.E_first) * (T)(nE - 1) / (T)(t.E_last - t.E_first));
+        int g;
+        if constexpr (sizeof(T) == 4) g = __float2int_ru((E - t.E_first) * t.inv_dE);
+        else g = (int)ceil((E - (T)t.E_first) * (T)t.inv_dE);
         g = g < 1 ? 1 : (g > nE - 1 ? nE - 1 : g);
         const uint16_t* gp = t.guide + (size_t)g * (MCD_GUIDE + 1) + kq;
         const T a = (T)__ldg(t.Es + g - 1), b = (T)__ldg(t.Es + g);
@@ -194,7 +197,7 @@ __device__ __forceinline__ T table_pick(const TableDev& t, T E, T U, bool* oor) 
             hi = __ldg(gp + 1);
         } else {
             lo = 0;
-            hi = t.nvalid ? __ldg(t.nvalid + i) : ncol;
+            hi = ncol;   // masked entries (0) act as +inf
         }
     }
     const float* row = t.cdf + (size_t)i * ncol;
