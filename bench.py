@@ -420,10 +420,24 @@ def adjoint_depth_bench(args, dev, p, n):
     d = 1e-3
     fdJ = (float(np.sum((m.chain(1 + d, 1.0)[0] - t) ** 2)) - float(np.sum((m.chain(1 - d, 1.0)[0] - t) ** 2))) / (2 * d)
     fdn = (float(np.sum((m.chain(1.0, 1 + d)[0] - t) ** 2)) - float(np.sum((m.chain(1.0, 1 - d)[0] - t) ** 2))) / (2 * d)
+    # dL/dJ is about 40 times smaller than dL/dn here, and an FP32 chain
+    # resolves a difference in J only to about 1e-2 of it (step 1e-3:
+    # rounding; step 1e-2: the curvature of the chain); the FP64 model on
+    # the first 1e5 electrons, adjoint against its own step-1e-5 difference
+    n64 = min(n, 100000)
+    m64 = ExitEnergyModel(p, n64, seed=args.seed, precision="fp64", device=dev, quantity="max_depth", lo=0.0,
+                          hi=20000.0, sigma=300.0)
+    t64, _, _ = m64.forward(1.1, 1.0)
+    h64, _, _ = m64.forward(1.0, 1.0)
+    dJ64, _ = m64.backward(2.0 * (h64 - t64), 0.0)
+    d64 = 1e-5
+    fdJ64 = (float(np.sum((m64.chain(1 + d64, 1.0)[0] - t64) ** 2)) -
+             float(np.sum((m64.chain(1 - d64, 1.0)[0] - t64) ** 2))) / (2 * d64)
     return {"fwd_ms": tf / args.steps, "bwd_ms": tb / args.steps, "bwd_over_fwd": tb / tf,
             "dL_dJscale": dJ, "dL_dnscale": dn, "fd_frozen_rel_err_J": abs(dJ - fdJ) / abs(fdJ) if fdJ else None,
             "fd_frozen_rel_err_n": abs(dn - fdn) / abs(fdn) if fdn else None, "fd_step": d,
-            "gpu_launches": 2 * args.steps}
+            "fp64_electrons": n64, "fp64_fd_frozen_rel_err_J": abs(dJ64 - fdJ64) / abs(fdJ64) if fdJ64 else None,
+            "gpu_launches": 2 * args.steps + 6}
 
 
 TABLES_WORKLOAD = ("the sampled-loss table pairs (Moller, outermost-shell Gryzinski) of the 16 (material, E0) "
