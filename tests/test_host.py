@@ -214,6 +214,10 @@ def test_new_fields_are_validated_before_any_gpu_work():
     t = _lib.Tune(256, 0, 1, 0, 5)
     assert L.mcd_run_batched(C.cast(host, C.c_void_p), 1, C.cast(host, C.c_void_p), C.byref(t),
                              C.cast(host, C.c_void_p), None) == _lib.EINVAL
+    # the 56-register kernel (variant bit 0) runs two blocks of at most 576 threads
+    t = _lib.Tune(640, 0, 1, 1, 0)
+    assert L.mcd_run_batched(C.cast(host, C.c_void_p), 1, C.cast(host, C.c_void_p), C.byref(t),
+                             C.cast(host, C.c_void_p), None) == _lib.EINVAL
     # a packed ring header holds electron indices below 2^28
     s = engine.make_sim(p, 2 ** 28 + 1)
     ring = _lib.EventRing(C.cast(host, C.c_void_p), 1, C.cast(host, C.c_void_p), _lib.EV_PACKED_HEAD, 0)
