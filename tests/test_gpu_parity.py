@@ -78,6 +78,18 @@ def test_fp64_tabulated_follows_oracle_trajectories(name, p, n):
     assert g.tally["bks"] + g.tally["abs"] + g.tally["trsm"] + g.tally["trdf"] + g.tally["long"] == n
 
 
+def test_fp64_table_on_a_range_bounded_by_powers_of_two():
+    """E0 = 8192 eV starts an octave block of its own and Emin = 1024 eV ends
+    the lowest one: the FP64 table still follows the oracle."""
+    p = input_par("Al", 8192.0, 1024.0, 20.0)
+    g, c = run_pair(p, 1500, seed=77, precision="fp64", tabulated=True)
+    e = g.electrons
+    same = (e["outcome"] == c["outcome"]) & (e["n_events"] == c["n_events"])
+    assert same.mean() >= 0.99, same.mean()
+    fe_ok = np.abs(e["final_E"] - c["final_E"]) <= 1e-9 * np.abs(c["final_E"])
+    assert (same & fe_ok).mean() >= 0.99
+
+
 def test_fp64_table_equals_inline_on_the_small_configuration():
     """The small FP64 configuration (Si 10 keV, 1000 electrons): with the
     table every trajectory matches the inline run's."""
