@@ -162,6 +162,9 @@ def sample_sizes(sims, electrons=CPU_SAMPLE_ELECTRONS):
     return [max(1, int(round(s["num_el"] * electrons / total))) for s in sims]
 
 
+_GOLDEN_TABLES = {}
+
+
 def oracle_tables(s):
     """The oracle's CDF tables of a workload simulation, on the W and E grids
     the reference's own grid search chose for it (tests/golden/tables.npz,
@@ -170,7 +173,9 @@ def oracle_tables(s):
     import coracle
     import mcd_oracle as O
     mat = O.Material(s["material"])
-    T = np.load(os.path.join(ROOT, "tests", "golden", "tables.npz"))
+    if "T" not in _GOLDEN_TABLES:
+        _GOLDEN_TABLES["T"] = np.load(os.path.join(ROOT, "tests", "golden", "tables.npz"))
+    T = _GOLDEN_TABLES["T"]
     key = "cfg4_%s_%d" % (s["material"], int(s["E0"] / 1000))
     spec = T[key + "/Moller/spec"]
     assert (spec[1], spec[2], spec[3]) == (s["Emin"], s["Wc"], s["tol_E"]), key
