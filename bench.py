@@ -384,7 +384,7 @@ def adjoint_bench(args, dev):
            "same_sequence_rel_err": abs(dJ - r["fd_same_sequence"]) / abs(dJ), "jump_part": r["fd_jump"],
            "jump_se_rel": r["jump_se"] / abs(dJ), "electrons_changed": r["changed"],
            "note": "the jump part is noise of standard error ~ 1/sqrt(N h) (16 seeds: mean 1.3% +- 2.9% of the "
-                   "gradient), so agreement is judged by z = (FD - adjoint) / its standard error"}
+                   "gradient), so agreement is measured by z = (FD - adjoint) / its standard error"}
     depth = adjoint_depth_bench(args, dev, p, n)
     return {"workload": ADJ_WORKLOAD, "num_el": n, "fwd_ms": tf / args.steps, "bwd_ms": tb / args.steps,
             "bwd_over_fwd": tb / tf, "loss": L, "dL_dJscale": dJ, "dL_dnscale": dn,

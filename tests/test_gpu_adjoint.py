@@ -72,10 +72,10 @@ def test_fp32_adjoint_against_fd_and_fp64():
 
 
 def test_full_resimulation_fd_is_close():
-    """The finite difference of the benchmark spec's check: central, relative
-    step 1e-3, common random numbers, every electron re-simulated at
-    J (1 +- 1e-3), at the size of the differentiable workload (Al 15 keV,
-    70 deg, 1e6 electrons, FP32).  Re-simulation lets about 0.35% of the
+    """The gradient check of the differentiable workload: a central finite
+    difference at relative step 1e-3 with common random numbers, every
+    electron re-simulated at J (1 +- 1e-3), at the workload's size (Al
+    15 keV, 70 deg, 1e6 electrons, FP32).  Re-simulation lets about 0.35% of the
     electrons change their exit event; their soft-bin terms jump, so the
     difference is the pathwise derivative plus a jump part whose standard
     error (from its independent per-electron terms) is about 10% of the

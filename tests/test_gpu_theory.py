@@ -14,8 +14,8 @@ W grid point (MC/tools/scattering.py:80-92), which at tol_W 1e-4 lowers the
 median Moller loss by about 1.5% (detectable at 2e4 samples; 0.1% here).
 
 Significance: every check is made on K = 10 independent subsamples (the
-electrons whose index is k mod 10), each tested at p > 0.01, the north
-star's level.  With no real difference the number of subsamples that
+electrons whose index is k mod 10), each tested at p > 0.01.  With no
+real difference the number of subsamples that
 reject is Binomial(10, 0.01); a check fails when more reject than its
 99.9% quantile allows (2), which a true match does with probability about
 1e-4.  The reference accepts U^2 < 0.152 (its 10% point) on 200-point
