@@ -147,7 +147,6 @@ def resimulated_fd(model, target, h=1e-3, param="J"):
     standard error of the jump part.  Returns a dict; the model keeps the
     checkpoints of (1, 1) afterwards."""
     torch = _torch()
-    dev = model.device
     t = np.asarray(target, dtype=np.float64)
     runs = []
     for x in (1.0 - h, 1.0 + h):
@@ -155,28 +154,48 @@ def resimulated_fd(model, target, h=1e-3, param="J"):
         hb, _, _ = model.forward(J, n)
         runs.append((hb.copy(), model.E_exit.to(torch.float64).clone(), model.kstar.clone()))
     (hm, qm, km), (hp, qp, kp) = runs
-    Lm, Lp = float(np.sum((hm - t) ** 2)), float(np.sum((hp - t) ** 2))
-    fd = (Lp - Lm) / (2.0 * h)
     hist = model.hist
-    cb = torch.as_tensor(hist.lo + (np.arange(model.nbins) + 0.5) * (hist.hi - hist.lo) / model.nbins,
-                         dtype=torch.float64, device=dev)
+    centers = hist.lo + (np.arange(model.nbins) + 0.5) * (hist.hi - hist.lo) / model.nbins
+    out = fd_split(qm, qp, km, kp, hm, hp, t, centers, hist.sigma, h, model.n)
+    model.forward(1.0, 1.0)
+    out.update(step=h, param=param)
+    return out
+
+
+def fd_split(qm, qp, km, kp, hm, hp, target, centers, sigma, h, n):
+    """Split the central difference (L(+) - L(-)) / 2h of
+    L = sum_b (h_b - t_b)^2 over the electrons.  qm/qp: per-electron
+    quantity of the two runs (torch tensors, any device), km/kp: their
+    recorded event (< 0 when the electron did not backscatter), hm/hp: the
+    runs' soft bins (normalised by n), centers: the bin centres c_b.  With
+    K_b(q) = exp(-(q - c_b)^2 / (2 sigma^2)) and hbar = (hm + hp) / 2,
+
+        L(+) - L(-) = sum_b (hp_b - hm_b) 2 (hbar_b - t_b),
+        hp_b - hm_b = (1/n) sum_e [K_b(qp_e) - K_b(qm_e)],
+
+    so electron e carries ce_e = sum_b [K_b(qp_e) - K_b(qm_e)] 2 (hbar_b - t_b) / (2 h n),
+    and the ce_e add up to the difference exactly when hm/hp are the soft
+    bins of qm/qp.  Host arithmetic on the tensors' own device; no kernel of
+    the transport runs here."""
+    import torch
+    dev = qm.device
+    t = np.asarray(target, dtype=np.float64)
+    fd = (float(np.sum((hp - t) ** 2)) - float(np.sum((hm - t) ** 2))) / (2.0 * h)
+    cb = torch.as_tensor(np.asarray(centers, dtype=np.float64), device=dev)
     g = torch.as_tensor(2.0 * (0.5 * (hm + hp) - t), dtype=torch.float64, device=dev)
-    inv2s2 = 1.0 / (2.0 * hist.sigma * hist.sigma)
-    ce = torch.empty(model.n, dtype=torch.float64, device=dev)
+    inv2s2 = 1.0 / (2.0 * sigma * sigma)
+    qm, qp = qm.to(torch.float64), qp.to(torch.float64)
+    ce = torch.empty(qm.shape[0], dtype=torch.float64, device=dev)
     step = 1 << 20
-    for a in range(0, model.n, step):
-        b = min(model.n, a + step)
+    for a in range(0, qm.shape[0], step):
+        b = min(qm.shape[0], a + step)
         kp_, km_ = (torch.exp(-(q[a:b, None] - cb[None, :]) ** 2 * inv2s2) @ g for q in (qp, qm))
         kp_ = torch.where(kp[a:b] >= 0, kp_, torch.zeros_like(kp_))
         km_ = torch.where(km[a:b] >= 0, km_, torch.zeros_like(km_))
-        ce[a:b] = (kp_ - km_) / (2.0 * h * model.n)
+        ce[a:b] = (kp_ - km_) / (2.0 * h * n)
     same = kp == km
-    fd_same = float(ce[same].sum())
-    fd_jump = float(ce[~same].sum())
-    jump_se = float(torch.sqrt((ce[~same] ** 2).sum()))
-    model.forward(1.0, 1.0)
-    return {"fd": fd, "fd_same_sequence": fd_same, "fd_jump": fd_jump, "jump_se": jump_se,
-            "changed": int((~same).sum()), "step": h, "param": param}
+    return {"fd": fd, "fd_same_sequence": float(ce[same].sum()), "fd_jump": float(ce[~same].sum()),
+            "jump_se": float(torch.sqrt((ce[~same] ** 2).sum())), "changed": int((~same).sum())}
 
 
 def _function():
