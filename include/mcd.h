@@ -413,9 +413,9 @@ int mcd_adjoint_chain(const mcd_sim* sim, const mcd_material* mat, const mcd_sof
  * in the reference.  Its scratch is a static device array sized for
  * MCD_STATIC_MAX_SIMS simulations (31.5 KiB), resident on every GPU that
  * loads the library until exit; more simulations return MCD_ETOOBIG.  The
- * first call on a device looks up that array's address (issue it before any
- * stream capture) and keeps it for the life of the device's primary
- * context: do not use the library across a cudaDeviceReset.  Calls share
+ * first call on a device looks up that array's address and keeps it for
+ * the life of the device's primary context: do not use the library across
+ * a cudaDeviceReset.  Calls share
  * the array: calls that overlap on the GPU race.  The simulations are
  * packed on the host and handed to a staging kernel on `stream` as one
  * kernel argument, so no host memory has to outlive the call;
