@@ -104,14 +104,23 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        """Start sampling every 100 ms; returns once the first sample is in
+        (at most 3 s), so that the samples kept cover the timed region from
+        its start."""
+        self.n0 = 0
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except OSError:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+            time.sleep(0.005)
+        self.n0 = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -127,7 +136,9 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        # the samples taken inside the timed region (the one before it when
+        # the region was shorter than a sampling interval)
+        for ln in self.lines[self.n0:] or self.lines[-1:]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 8:
                 continue
