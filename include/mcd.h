@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCD_ABI_VERSION 9
+#define MCD_ABI_VERSION 10
 #define MCD_MAX_SHELLS 8
 #define MCD_MAX_CHANNELS 16
 #define MCD_HIST_E_MAX 256
@@ -287,12 +287,15 @@ int mcd_build_table(int kind, const mcd_material* mat, int shell,
  * (Ruth, Moller, Gryzinski shells), stored as FP32 and interpolated
  * linearly (within 3e-7 of the exact sums) -- the table the batched path
  * builds per group of simulations.
- * FP64: the same sums stored as FP64 on grids uniform in E inside each
+ * FP64: the mean free path and the running sums as fractions of the
+ * total, as FP64 cubics in the cells of grids uniform in E inside each
  * octave of (Emin, E0] (256 cells per octave, indexed from the exponent and
- * mantissa bits of E), interpolated by the cubic through four nodes (within
- * about 4e-10 of the exact sums); cells whose nodes straddle a channel
- * threshold are flagged and evaluated exactly.  The octaves must fit the
- * buffer: MCD_ETOOBIG otherwise (Au from 0.5 to 30 keV fits).
+ * mantissa bits of E; per cell four coefficients per column, through the
+ * values at four nodes; within about 1.3e-10 of the exact values); cells
+ * whose nodes straddle a channel threshold, or reach below 2 Wc (where the
+ * Moller cross section turns negative towards its pole at Wc), are flagged
+ * and evaluated exactly.  The octaves must fit the buffer: MCD_ETOOBIG otherwise (Au
+ * from 50 eV to 30 keV fits, from 10 eV does not).
  * It depends on the material, Wc, the elastic model, n_scale, E0, Emin and
  * the precision.  table is 16-byte-aligned device memory of
  * mcd_sigma_table_bytes() bytes.                                            */

@@ -106,10 +106,10 @@ struct __align__(16) SimConst {
     // padding FLT_MAX).  The total and the first sums share one 16-byte load.
     // E * sigma varies slowly in log E, so linear interpolation at 128 rows
     // per octave is within 3e-7 of the exact sums (relative to the total).
-    // FP64 transport reads an FP64 table (the octave blocks described at
-    // kSig64Cells) through the same pointer: sig_l0 then holds the first
-    // octave's exponent, sig_rows the number of octaves and sig_S the row
-    // stride in doubles (sig_K + 1, the flag last).
+    // FP64 transport reads an FP64 table (the octave blocks of cell records
+    // described at kSig64Cells) through the same pointer: sig_l0 then holds
+    // the first octave's exponent and sig_rows the number of octaves; the
+    // record stride is sig64_stride(sig_K) doubles.
     const void* sig;
     float sig_l0, sig_inv, sig_tmax, sig_off;   // sig_off = -sig_l0 * sig_inv
     int32_t sig_K, sig_S, sig_rows;
@@ -133,20 +133,32 @@ constexpr int kSigStride = 12;         // floats per row, at most (3 + MCD_MAX_S
 constexpr double kSigPerOctave = 128;  // grid density
 
 // FP64 cross-section tables (FP64 DS transport reading mcd_sim.sigma_table):
-// one block of kSig64Rows rows per octave [2^e, 2^(e+1)) of the energy range,
-// uniform in E inside the octave: kSig64Cells cells of 2^e / kSig64Cells eV,
-// with one node below the octave and two above it, so that the cubic
-// through the nodes i-1 .. i+2 (block rows i .. i+3) serves cell i.  A row
-// holds E times the total, E times the running sums in pick order (Ruth,
-// +Moller, +Gryz[k] ...), then a flag: 1 when a channel threshold (a shell's
-// binding energy, Wc, the plasmon energy) lies inside the cell's four-node
-// span, where the transport evaluates the cross sections instead (they have
-// a kink there).  The octave is the exponent of E and the position inside it
-// the mantissa, so the index needs no logarithm and is exact; the cubic is
-// within about 4e-10 of the exact sums (relative to the total) away from
-// thresholds for Al, Si, Cu and Au over 0.5-30 keV.
+// one block of kSig64Cells cell records per octave [2^e, 2^(e+1)) of the
+// energy range, uniform in E inside the octave: cell i covers
+// 2^e [1 + i / cells, 1 + (i + 1) / cells), so that the octave is the
+// exponent of E, the cell the top mantissa bits and the offset f in [0, 1)
+// the remaining ones (no logarithm, exact).  A record holds a flag word (1
+// when a channel threshold -- a shell's binding energy, Wc, the plasmon
+// energy -- lies in the span of the four nodes i - 1 .. i + 2, where the
+// cross sections have a kink, or the lowest node lies below 2 Wc, where the
+// Moller cross section is negative with a pole at Wc; the transport
+// evaluates the cross sections there instead), a
+// pad word, then for each of the sig_K columns the coefficients c0..c3 of
+// the cubic c0 + f (c1 + f (c2 + f c3)) through the column's values at those
+// four nodes: column 0 the mean free path 1 / sum(sigma) in A, columns
+// 1 .. sig_K - 1 the running sums in pick order (Ruth, +Moller, +Gryz[k]
+// ...) as fractions of the total.  The event then needs no division and no
+// interpolation weights: three FMAs per column read, the channel the first
+// fraction at or above U.  In the unflagged cells the cubic is within about
+// 1.3e-10 of the exact mean free path (relative) and of the exact fractions
+// (absolute) for Al, Si, Cu and Au over 0.1-30 keV.
 constexpr int kSig64Cells = 256;
-constexpr int kSig64Rows = kSig64Cells + 3;
+__host__ __device__ constexpr int sig64_stride(int K) { return 2 + 4 * K; }   // doubles per cell record
+
+// Bytes of a caller's cross-section table buffer (mcd_sigma_table_bytes):
+// FP32 tables take at most kSigRowsMax rows of kSigStride floats (192 KiB);
+// FP64 tables take whole octaves, 920 KiB for Au from 50 eV to 30 keV.
+constexpr size_t kSigTableBytes = (size_t)1 << 20;
 
 // First octave exponent and octave count of an FP64 table over (lo, hi].
 inline int sigma_octaves64(double lo, double hi, int32_t* e_lo) {
@@ -157,10 +169,10 @@ inline int sigma_octaves64(double lo, double hi, int32_t* e_lo) {
     return b - a + 1;
 }
 
-// Bytes of the FP64 table of a simulation (K channel columns + the flag).
+// Bytes of the FP64 table of a simulation with K channel columns.
 inline size_t sigma_bytes64(double lo, double hi, int K) {
     int32_t e0 = 0;
-    return sizeof(double) * (size_t)sigma_octaves64(lo, hi, &e0) * kSig64Rows * (size_t)(K + 1);
+    return sizeof(double) * (size_t)sigma_octaves64(lo, hi, &e0) * kSig64Cells * (size_t)sig64_stride(K);
 }
 
 // The log2-E grid of a cross-section table over [lo, hi] (eV), slightly
@@ -281,7 +293,6 @@ inline SimConst<T> make_consts(const mcd_sim& s, const mcd_material& m,
             int32_t e0 = 0;
             c.sig_rows = sigma_octaves64(s.Emin, s.E0, &e0);
             c.sig_l0 = (float)e0;
-            c.sig_S = c.sig_K + 1;
         } else {
             sigma_grid(s.Emin, s.E0, &c.sig_l0, &c.sig_inv, &c.sig_tmax, &c.sig_rows);
             c.sig_off = -c.sig_l0 * c.sig_inv;
@@ -306,7 +317,7 @@ inline int check_sim(const mcd_sim& s, const mcd_material& m, const mcd_table* t
     // an FP64 table must fit the mcd_sigma_table_bytes() a caller allocates
     if (s.sigma_table && s.precision == MCD_FP64 && m.n_shells >= 0 && m.n_shells <= MCD_MAX_SHELLS &&
         s.E0 > s.Emin && s.Emin > 0 &&
-        sigma_bytes64(s.Emin, s.E0, m.n_shells + 3) > sizeof(float) * (size_t)kSigRowsMax * kSigStride)
+        sigma_bytes64(s.Emin, s.E0, m.n_shells + 3) > kSigTableBytes)
         return MCD_ETOOBIG;
     if (!(s.E0 > s.Emin) || !(s.Emin > 0)) return MCD_EINVAL;
     if (s.num_el < 0) return MCD_EINVAL;

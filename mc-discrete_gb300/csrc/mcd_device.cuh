@@ -160,8 +160,13 @@ __device__ __forceinline__ void sincospi_uniform(double u, double* s, double* c)
 
 template <>
 struct Ops<double> {
-    static __device__ __forceinline__ double unit(uint32_t u) { return ((double)u + 0.5) * 0x1p-32; }
-    static __device__ __forceinline__ double unit_c(uint32_t u) { return ((double)(~u) + 0.5) * 0x1p-32; }
+    // (u + 1/2) 2^-32, built as the double 1 + (u + 1/2) 2^-32 (u in the top
+    // 32 mantissa bits, the half below them) less 1: exact, one FP64
+    // subtraction instead of a conversion, an addition and a product
+    static __device__ __forceinline__ double unit(uint32_t u) {
+        return __hiloint2double(0x3ff00000 | (int)(u >> 12), (int)((u << 20) | 0x80000u)) - 1.0;
+    }
+    static __device__ __forceinline__ double unit_c(uint32_t u) { return unit(~u); }
     static __device__ __forceinline__ double ln(double x) { return log(x); }
     // the step's uniform and the azimuth's: table driven (ln_uniform,
     // sincospi_uniform above), 12% and 10% of the small FP64 configuration's
@@ -397,12 +402,16 @@ __device__ __forceinline__ void lane_lose(Lane<T>& L, const C& c, T W) {
 // the rotation q p q* written out (equal to it within rounding).
 template <class T, class C>
 __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_phi) {
-    const T st = Ops<T>::sqrt_(s2);
-    const T ct = Ops<T>::sqrt_((T)1 - s2);
+    // sin(theta) = 2 sin(theta/2) cos(theta/2); FP64 takes it as
+    // 2 sqrt(s2 (1 - s2)), one square root on the narrow FP64 unit, while
+    // FP32 keeps the two roots (one root measured no faster there)
+    T sth;
+    if constexpr (sizeof(T) == 8) sth = (T)2 * Ops<T>::sqrt_(s2 * ((T)1 - s2));
+    else sth = (T)2 * Ops<T>::sqrt_(s2) * Ops<T>::sqrt_((T)1 - s2);
     T sp, cp;
     Ops<T>::sincos_pi(u_phi, &sp, &cp);
     if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
-    const T cth = (T)1 - (T)2 * s2, sth = (T)2 * st * ct;
+    const T cth = (T)1 - (T)2 * s2;
     const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
     const T xx = L.yy * L.dz - L.yz * L.dy;
     const T xy = L.yz * L.dx - L.yx * L.dz;
@@ -472,44 +481,49 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
     return MCD_CH_GRYZ0 + (j - 2);
 }
 
-// The same from an FP64 table (FP64 transport; layout at kSig64Cells): the
-// octave block from the exponent bits of E, the cell and its offset from
-// the mantissa bits (exact), and the cubic through the cell's four nodes in
-// each column.  Returns -1 for a cell whose nodes straddle a channel
-// threshold (its flag is set): the caller evaluates the cross sections.
+// The channel and the mean free path from an FP64 table (FP64 transport;
+// layout at kSig64Cells): the octave from the exponent bits of E, the cell
+// from the top mantissa bits and its offset f from the other 44 (exact, by
+// integer operations and one subtraction), then each column read is three
+// FMAs.  The FP64 unit is narrow on this GPU and busy for the whole warp
+// however few lanes are active, so the lookup is built to issue few FP64
+// instructions: no logarithm, no interpolation weights, no division.  With
+// diffraction (a constant cross section dS) the total grows by the factor
+// g = 1 + dS lambda; the event diffracts when U g > 1, otherwise U g is
+// compared with the fractions of the other channels.  Returns -1 for a cell
+// whose nodes straddle a channel threshold (its flag is set): the caller
+// evaluates the cross sections.
 template <class C>
-__device__ __forceinline__ int tab_pick64(const C& c, double E, double U, double* Etot_out) {
-    const long long b = __double_as_longlong(E);
-    const int ex = (int)((b >> 52) & 0x7ff) - 1023;
-    const double m = __longlong_as_double((b & 0x000fffffffffffffll) | 0x3ff0000000000000ll);   // [1, 2)
-    const double t = (m - 1.0) * (double)kSig64Cells;                                           // exact
-    int i = (int)t;
-    const double f = t - (double)i;
-    int blk = ex - (int)c.sig_l0;
+__device__ __forceinline__ int tab_pick64(const C& c, double E, double U, double* mfp_out) {
+    const long long b = __double_as_longlong(E);   // E > 0
+    int blk = (int)(b >> 52) - 1023 - (int)c.sig_l0;
     blk = blk < 0 ? 0 : (blk > c.sig_rows - 1 ? c.sig_rows - 1 : blk);
-    i = i > kSig64Cells - 1 ? kSig64Cells - 1 : i;
-    const int S = bits_S(c), K = bits_K(c);
-    const double* r = static_cast<const double*>(c.sig) + ((size_t)blk * kSig64Rows + i) * S;
-    if (__ldg(r + K) != 0.0) return -1;
-    // Lagrange weights of the nodes at -1, 0, 1, 2 (in cells) for offset f
-    const double fp1 = f + 1.0, fm1 = f - 1.0, fm2 = f - 2.0;
-    const double w0 = -f * fm1 * fm2 * (1.0 / 6.0);
-    const double w1 = 0.5 * fp1 * fm1 * fm2;
-    const double w2 = -0.5 * fp1 * f * fm2;
-    const double w3 = fp1 * f * fm1 * (1.0 / 6.0);
+    const int i = (int)(b >> 44) & (kSig64Cells - 1);
+    const double f = __longlong_as_double(((b << 8) & 0x000fffffffffff00ll) | 0x3ff0000000000000ll) - 1.0;
+    const int K = bits_K(c);
+    const double* r = static_cast<const double*>(c.sig) + ((size_t)blk * kSig64Cells + i) * sig64_stride(K);
+    if (__ldg(reinterpret_cast<const long long*>(r)) != 0ll) return -1;
     auto at = [&](int col) {
-        return fma(w0, __ldg(r + col), fma(w1, __ldg(r + S + col), fma(w2, __ldg(r + 2 * S + col), w3 * __ldg(r + 3 * S + col))));
+        const double2 lo = __ldg(reinterpret_cast<const double2*>(r + 2 + 4 * col));
+        const double2 hi = __ldg(reinterpret_cast<const double2*>(r + 4 + 4 * col));
+        return fma(fma(fma(hi.y, f, hi.x), f, lo.y), f, lo.x);
     };
-    const double tot = at(0);
-    double all = tot;
-    if (c.bits & kBitDiff) all = fma(E, (double)c.dS, tot);   // + diffraction
-    *Etot_out = all;
-    const double target = U * all;
-    if ((c.bits & kBitDiff) && target > tot) return MCD_CH_DIFF;
-    // the first running sum at or above the target names the channel (most
+    double mfp = at(0);
+    double u = U;
+    if (c.bits & kBitDiff) {
+        const double g = fma((double)c.dS, mfp, 1.0);
+        u = U * g;
+        mfp = mfp / g;
+        if (u > 1.0) {
+            *mfp_out = mfp;
+            return MCD_CH_DIFF;
+        }
+    }
+    *mfp_out = mfp;
+    // the first running-sum fraction at or above u names the channel (most
     // events stop at the Rutherford column)
     int j = 0;
-    while (j < K - 1 && at(j + 1) < target) ++j;
+    while (j < K - 1 && at(j + 1) < u) ++j;
     if (j == 0) return MCD_CH_RUTH;
     if (j == 1) return MCD_CH_MOLLER;
     if (j == K - 1) return MCD_CH_QUINN;
@@ -546,9 +560,9 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
             ch = tab_pick(c, (float)E, (float)Ops<T>::unit(r.x), &Etot);
             inv_tot = Ops<T>::div(E, (T)Etot);
         } else {
-            double Etot;
-            ch = tab_pick64(c, E, Ops<T>::unit(r.x), &Etot);
-            if (ch >= 0) inv_tot = E / Etot;
+            double mfp;
+            ch = tab_pick64(c, E, Ops<T>::unit(r.x), &mfp);
+            if (ch >= 0) inv_tot = mfp;
             else use_tab = false, ch = MCD_CH_QUINN;   // a threshold inside the cell
         }
     }

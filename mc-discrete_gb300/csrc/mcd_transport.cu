@@ -404,37 +404,55 @@ __global__ void __launch_bounds__(256) k_sigtab_one(const SimConst<double> c, fl
 }
 
 // The FP64 table of one simulation (mcd_build_sigma_table for FP64
-// transport; layout at kSig64Cells): one thread per (octave block, row).
-// Block row q of octave e holds node q - 1 at E = 2^e (1 + (q - 1) / cells),
-// and its flag marks cell q, whose cubic spans nodes q - 1 .. q + 2.
-__global__ void __launch_bounds__(256) k_sigtab64(const SimConst<double> c, int e_lo, int blocks, int S,
+// transport; layout at kSig64Cells): one thread per (octave, cell).  It
+// evaluates the mean free path and the running-sum fractions at the cell's
+// four nodes E_n = 2^e (1 + (i - 1 + n) / cells), n = 0..3, and stores the
+// coefficients of the cubic through them in the offset f = (E - E_1) / h:
+// with v_n the node values, c0 = v_1, c1 = -v_0/3 - v_1/2 + v_2 - v_3/6,
+// c2 = v_0/2 - v_1 + v_2/2, c3 = (v_3 - v_0)/6 + (v_1 - v_2)/2 (the
+// Lagrange cubic written in powers of f).
+__global__ void __launch_bounds__(128) k_sigtab64(const SimConst<double> c, int e_lo, int blocks,
                                                    double* table) {
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= blocks * kSig64Rows) return;
-    const int blk = gid / kSig64Rows, q = gid % kSig64Rows;
+    if (gid >= blocks * kSig64Cells) return;
+    const int blk = gid / kSig64Cells, i = gid % kSig64Cells;
+    const int K = c.nsh + 3;
     const double base = ldexp(1.0, e_lo + blk), h = base / kSig64Cells;
-    const double E = base + (double)(q - 1) * h;
-    double* row = table + (size_t)gid * S;
-    const double invE = 1.0 / E;
-    double cum = sig_ruth<double>(c, E);
-    int col = 1;
-    row[col++] = E * cum;
-    cum += sig_moller<double>(c, E, invE);
-    row[col++] = E * cum;
-    for (int k = 0; k < c.nsh; ++k) {
-        cum += sig_gryz<double>(c, E, invE, k);
-        row[col++] = E * cum;
+    double v[4][3 + MCD_MAX_SHELLS];
+    for (int n = 0; n < 4; ++n) {
+        const double E = base + (double)(i - 1 + n) * h;
+        const double invE = 1.0 / E;
+        double run[3 + MCD_MAX_SHELLS];
+        double cum = sig_ruth<double>(c, E);
+        run[1] = cum;
+        cum += sig_moller<double>(c, E, invE);
+        run[2] = cum;
+        for (int k = 0; k < c.nsh; ++k) {
+            cum += sig_gryz<double>(c, E, invE, k);
+            run[3 + k] = cum;
+        }
+        cum += sig_quinn<double>(c, E, invE);
+        const double inv = 1.0 / cum;
+        v[n][0] = inv;
+        for (int k = 1; k < K; ++k) v[n][k] = run[k] * inv;
     }
-    cum += sig_quinn<double>(c, E, invE);
-    row[0] = E * cum;
-    bool kink = false;
-    if (q < kSig64Cells) {
-        const double lo = E, hi = E + 3.0 * h;
-        auto in = [&](double x) { return x >= lo && x <= hi; };
-        kink = in(c.Wc) || in(c.Epl);
-        for (int k = 0; k < c.nsh; ++k) kink |= in(c.gEs[k]);
+    double* rec = table + (size_t)gid * sig64_stride(K);
+    const double E1 = base + (double)(i - 1) * h, E4 = E1 + 3.0 * h;
+    auto in = [&](double x) { return x >= E1 && x <= E4; };
+    // below 2 Wc the Moller cross section is negative and falls to -inf at
+    // Wc (MC/tools/crossSections.py:183-208), which no cubic follows
+    bool kink = in(c.Wc) || in(c.Epl) || E1 < 2.0 * c.Wc;
+    for (int k = 0; k < c.nsh; ++k) kink |= in(c.gEs[k]);
+    rec[0] = kink ? 1.0 : 0.0;
+    rec[1] = 0.0;
+    for (int k = 0; k < K; ++k) {
+        const double a = v[0][k], b = v[1][k], d = v[2][k], e = v[3][k];
+        double* q = rec + 2 + 4 * k;
+        q[0] = b;
+        q[1] = -a / 3.0 - b / 2.0 + d - e / 6.0;
+        q[2] = a / 2.0 - b + d / 2.0;
+        q[3] = (e - a) / 6.0 + (b - d) / 2.0;
     }
-    row[S - 1] = kink ? 1.0 : 0.0;
 }
 
 // Do two simulations have the same channel cross sections at every energy?
@@ -573,7 +591,7 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
                                  st);
 }
 
-extern "C" size_t mcd_sigma_table_bytes(void) { return batch_sig_bytes(); }
+extern "C" size_t mcd_sigma_table_bytes(void) { return kSigTableBytes; }
 
 extern "C" int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat, void* table, void* stream) {
     if (!sim || !mat || !table) return MCD_EINVAL;
@@ -583,16 +601,15 @@ extern "C" int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat
     if (!(sim->E0 > sim->Emin) || !(sim->Emin > 0) || !(sim->Wc > 0)) return MCD_EINVAL;
     if (mat->n_shells < 0 || mat->n_shells > MCD_MAX_SHELLS || mat->atnd <= 0) return MCD_EINVAL;
     if ((reinterpret_cast<uintptr_t>(table) & 15) != 0) return MCD_EINVAL;   // rows are read as float4
-    if (sim->precision == MCD_FP64 && sigma_bytes64(sim->Emin, sim->E0, mat->n_shells + 3) > batch_sig_bytes())
+    if (sim->precision == MCD_FP64 && sigma_bytes64(sim->Emin, sim->E0, mat->n_shells + 3) > kSigTableBytes)
         return MCD_ETOOBIG;
     mcd_sim s = *sim;
     s.sigma_table = table;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (sim->precision == MCD_FP64) {
         const SimConst<double> c = make_consts<double>(s, *mat, nullptr, nullptr);
-        const int n = c.sig_rows * kSig64Rows;
-        k_sigtab64<<<(n + 255) / 256, 256, 0, st>>>(c, (int)c.sig_l0, c.sig_rows, c.sig_S,
-                                                     static_cast<double*>(table));
+        const int n = c.sig_rows * kSig64Cells;
+        k_sigtab64<<<(n + 127) / 128, 128, 0, st>>>(c, (int)c.sig_l0, c.sig_rows, static_cast<double*>(table));
         return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
     }
     s.precision = MCD_FP32;

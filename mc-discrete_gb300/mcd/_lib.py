@@ -9,7 +9,7 @@ import os
 
 from . import build as _build
 
-ABI_VERSION = 9
+ABI_VERSION = 10
 MAX_SHELLS = 8
 GUIDE = 256
 MAX_CHANNELS = 16

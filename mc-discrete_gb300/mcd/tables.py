@@ -261,21 +261,29 @@ def ds_tables(mat, E0, Emin, Wc, tol_E, tol_W, device="cuda"):
 _SIG_CACHE = {}
 
 
-SIG64_CELLS, SIG64_ROWS = 256, 259
+SIG64_CELLS = 256
+
+
+def sig64_stride(n_channels):
+    """Doubles per cell record of an FP64 table: a flag word, a pad word and
+    four cubic coefficients per column."""
+    return 2 + 4 * n_channels
 
 
 def sigma_table_fits(sim, mat):
     """Does the FP64 table of this simulation's energy range fit the buffer
-    (mcd_sigma_table_bytes)?  One block of 259 rows of n_shells + 4 doubles
-    per octave of (Emin, E0]."""
+    (mcd_sigma_table_bytes)?  One block of 256 cell records per octave of
+    (Emin, E0], each of 2 + 4 (n_shells + 3) doubles."""
     octaves = math.frexp(float(sim.E0))[1] - math.frexp(float(sim.Emin))[1] + 1
-    return 8 * octaves * SIG64_ROWS * (mat.n_shells + 4) <= _lib.lib().mcd_sigma_table_bytes()
+    return 8 * octaves * SIG64_CELLS * sig64_stride(mat.n_shells + 3) <= _lib.lib().mcd_sigma_table_bytes()
 
 
 def sigma_table(sim, mat, device="cuda"):
     """Device cross-section table of a DS simulation for its precision
-    (mcd_build_sigma_table: E times the total and running channel cross
-    sections over [Emin, E0]; FP32 on a log2-E grid, FP64 on octave grids),
+    (mcd_build_sigma_table over [Emin, E0]: FP32, E times the total and the
+    running channel cross sections on a log2-E grid; FP64, the mean free
+    path and the running sums as fractions of the total, cubics on octave
+    grids),
     cached per material, Wc, elastic model, density scale, energy range and
     precision."""
     import torch

@@ -7,11 +7,15 @@ log/sin and glibc's differ in the last bit right at a decision boundary,
 hence the 99% floor).  FP32 transport is checked against the oracle
 statistically and by its per-electron agreement rate.
 """
+import math
+
+import mcd_oracle as O
 import numpy as np
 import pytest
+import torch
 from scipy import stats
 
-from mcd import engine
+from mcd import _lib, engine, tables
 from _gpu_util import eta_z, input_par, run_pair
 
 pytestmark = pytest.mark.gpu
@@ -61,10 +65,10 @@ DS_CASES = [c for c in CASES if "_ds" in c[0] or c[0] == "si_film_diff"]
 
 @pytest.mark.parametrize("name,p,n", DS_CASES, ids=[c[0] for c in DS_CASES])
 def test_fp64_tabulated_follows_oracle_trajectories(name, p, n):
-    """FP64 transport reading its FP64 cross-section table (cubic on octave
-    grids, within about 4e-10 of the exact sums; exact where a channel
-    threshold lies in the cell) follows the oracle like the inline path:
-    a channel decision moves only when a draw falls that close to a
+    """FP64 transport reading its FP64 cross-section table (cubics on
+    octave grids, within about 1.3e-10 of the exact values; exact where a
+    channel threshold lies in the cell) follows the oracle like the inline
+    path: a channel decision moves only when a draw falls that close to a
     boundary."""
     g, c = run_pair(p, n, seed=123, precision="fp64", tabulated=True)
     e = g.electrons
@@ -76,6 +80,55 @@ def test_fp64_tabulated_follows_oracle_trajectories(name, p, n):
     d_ok |= np.isnan(c["dir"]).any(axis=1) & np.isnan(e["dir"]).any(axis=1)
     assert (same & d_ok).mean() >= 0.99, name
     assert g.tally["bks"] + g.tally["abs"] + g.tally["trsm"] + g.tally["trdf"] + g.tally["long"] == n
+
+
+SIG64_CASES = [("Si", 100.0, 100.0), ("Al", 100.0, 100.0), ("Cu", 100.0, 100.0), ("Au", 100.0, 50.0)]
+
+
+@pytest.mark.parametrize("sp,Emin,Wc", SIG64_CASES, ids=[c[0] for c in SIG64_CASES])
+def test_fp64_sigma_table_against_the_oracle_cross_sections(sp, Emin, Wc):
+    """The FP64 table mcd_build_sigma_table writes, read back and evaluated
+    on the host as the transport reads it (octave from the exponent, cell
+    and offset from the mantissa, Horner in each column), against the
+    oracle's cross sections at 3000 seeded energies over (Emin, 30 keV]: the
+    mean free path within 3e-10 relative and the running-sum fractions
+    within 3e-10 absolute in every unflagged cell, and a cell is flagged
+    exactly when a channel threshold lies in the span of its four nodes or
+    its lowest node lies below 2 Wc (the Moller cross section is negative
+    there, with a pole at Wc)."""
+    p = input_par(sp, 30000.0, Emin, 0.0, Wc=Wc)
+    mat = _lib.material(sp)
+    sim = engine.make_sim(p, 16, precision=_lib.FP64)
+    assert tables.sigma_table_fits(sim, mat)
+    tab = tables.sigma_table(sim, mat).view(torch.float64).cpu().numpy()
+    om = O.Material(sp)
+    K = 3 + len(om.shells)
+    stride = tables.sig64_stride(K)
+    e_lo = math.frexp(Emin)[1] - 1
+    thresholds = [Wc, om.plasmon_e] + [Es for _, Es, _ in om.shells]
+    rng = np.random.default_rng(11)
+    worst_mfp, worst_frac, flagged = 0.0, 0.0, 0
+    for E in np.exp(rng.uniform(math.log(Emin), math.log(30000.0), 3000)):
+        m, ex = math.frexp(E)          # E = m 2^ex, m in [0.5, 1)
+        t = (2.0 * m - 1.0) * tables.SIG64_CELLS
+        i = int(t)
+        f = t - i
+        rec = tab[((ex - 1 - e_lo) * tables.SIG64_CELLS + i) * stride:][:stride]
+        h = 2.0 ** (ex - 1) / tables.SIG64_CELLS
+        E1 = 2.0 ** (ex - 1) + (i - 1) * h
+        kink = any(E1 <= x <= E1 + 3 * h for x in thresholds) or E1 < 2 * Wc
+        assert (rec[0] != 0.0) == kink, (sp, E)
+        if kink:
+            flagged += 1
+            continue
+        c = rec[2:].reshape(K, 4)
+        val = ((c[:, 3] * f + c[:, 2]) * f + c[:, 1]) * f + c[:, 0]
+        sig = [v for _, v in O.ds_sigmas(E, om, Wc)]
+        tot = sum(sig)
+        worst_mfp = max(worst_mfp, abs(val[0] / O.mfp_from_sigma(tot, om.atnd) - 1.0))
+        worst_frac = max(worst_frac, float(np.max(np.abs(val[1:] - np.cumsum(sig)[:-1] / tot))))
+    assert worst_mfp < 3e-10 and worst_frac < 3e-10, (sp, worst_mfp, worst_frac)
+    assert flagged < 450     # 100-200 eV (below 2 Wc) is about 12% of the log-uniform energies
 
 
 def test_fp64_table_on_a_range_bounded_by_powers_of_two():

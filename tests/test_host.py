@@ -39,7 +39,7 @@ def test_struct_layouts_match():
 
 def test_abi_and_errors():
     L = _lib.lib()
-    assert L.mcd_abi_version() == _lib.ABI_VERSION == 9
+    assert L.mcd_abi_version() == _lib.ABI_VERSION == 10
     assert L.mcd_strerror(_lib.EINVAL) == b"invalid argument"
     m = _lib.Material()
     assert L.mcd_material_init(b"Fe", C.byref(m)) == _lib.ENOSPECIES
@@ -198,12 +198,14 @@ def test_new_fields_are_validated_before_any_gpu_work():
     s.sigma_table = C.addressof(C.c_float(0.0))
     assert L.mcd_run(C.byref(s), C.byref(mat), None, None, 1, None, None, 1, 128, None) == _lib.EINVAL
     assert L.mcd_build_sigma_table(C.byref(s), C.byref(mat), None, None) == _lib.EINVAL
-    assert L.mcd_sigma_table_bytes() == 4 * 4096 * 12
-    # an FP64 table covers whole octaves of (Emin, E0]: 100 eV to 30 keV for
-    # Au (nine octaves of 259 rows x 12 doubles) exceeds the buffer; the
+    assert L.mcd_sigma_table_bytes() == 1 << 20
+    # an FP64 table covers whole octaves of (Emin, E0]: 10 eV to 30 keV for
+    # Au (twelve octaves of 256 cells x 46 doubles) exceeds the buffer; the
     # size is checked before any launch
     au = _lib.material("Au")
-    s = engine.make_sim(dict(material="Au", E0=30000.0, Emin=100.0, Wc=50.0, mode="DS"), 16, precision=_lib.FP64)
+    assert 8 * 12 * 256 * tables.sig64_stride(au.n_shells + 3) > L.mcd_sigma_table_bytes()
+    assert 8 * 10 * 256 * tables.sig64_stride(au.n_shells + 3) <= L.mcd_sigma_table_bytes()   # from 50 eV
+    s = engine.make_sim(dict(material="Au", E0=30000.0, Emin=10.0, Wc=50.0, mode="DS"), 16, precision=_lib.FP64)
     tbl = (C.c_double * 4)()
     addr = (C.addressof(tbl) + 15) & ~15            # 16-byte aligned, as the entry point requires
     assert L.mcd_build_sigma_table(C.byref(s), C.byref(au), C.c_void_p(addr), None) == _lib.ETOOBIG
