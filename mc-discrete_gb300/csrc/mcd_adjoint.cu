@@ -62,7 +62,7 @@ template <class T, class C>
 __device__ __forceinline__ T step_len(const C& c, T E, uint64_t elec, int64_t k) {
     const uint4 r = philox(make_uint4((uint32_t)k, (uint32_t)elec, (uint32_t)(elec >> 32), c.sim_id), c.key0,
                            c.key1);
-    return -Ops<T>::ln_step(Ops<T>::unit(r.y)) * Ops<T>::div((T)1, sig_ruth<T>(c, E));
+    return -Ops<T>::ln_step_word(r.y) * Ops<T>::div((T)1, sig_ruth<T>(c, E));
 }
 
 // dS/dE and dS/dJ_scale of the Bethe law at E (S itself returned in *S)

@@ -55,7 +55,7 @@ struct Ops<float> {
     // logarithm of the step-length draw: the special-function unit's log2,
     // absolute error <= 2^-22 for x in [1/2, 2] and 2 ulp elsewhere, i.e. a
     // step of -ln U mean free paths is off by at most about 1e-7 of one
-    static __device__ __forceinline__ float ln_step(float x) { return __logf(x); }
+    static __device__ __forceinline__ float ln_step_word(uint32_t w) { return __logf(unit(w)); }
     static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
     static __device__ __forceinline__ float rsqrt_(float x) { return rsqrtf(x); }
     // 1/sqrt(x) for the squared norm of a rotated unit vector
@@ -65,6 +65,7 @@ struct Ops<float> {
     static __device__ __forceinline__ void sincos_pi(float u, float* s, float* c) {
         __sincosf(3.14159265358979f * u, s, c);
     }
+    static __device__ __forceinline__ void sincos_pi_word(uint32_t w, float* s, float* c) { sincos_pi(unit(w), s, c); }
     static __device__ __forceinline__ float nan_() { return __int_as_float(0x7fc00000); }
     static __device__ __forceinline__ float acos_deg(float x) { return acosf(x) * 57.2957795f; }
 };
@@ -76,9 +77,9 @@ struct Ops<float> {
 // 1990: a table at 256 breakpoints and a short series of the remainder).
 // The arguments are uniforms in (0, 1) with 33 significant bits, and what a
 // trajectory needs is absolute accuracy, since a step's error enters the
-// position as that error times the mean free path: about 1e-16 for the
-// logarithm (relative 2e-16 where |ln U| >= ln 2) and for sin/cos.  The
-// tables are evaluated at compile time from their own series.
+// position as that error times the mean free path: within one ulp, i.e.
+// 2.3e-16 max(1, |ln U|) for the logarithm and 1.2e-16 for sin/cos
+// (against 40-digit values in the tests).
 // ---------------------------------------------------------------------------
 struct F64Tabs {
     double lnm[256];    // ln(1 + j/256)
@@ -86,40 +87,75 @@ struct F64Tabs {
     double sn[256];     // sin(pi j/256)
     double cs[256];     // cos(pi j/256)
 };
+// The table entries are evaluated at compile time in double-double
+// arithmetic (T. J. Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18, 1971: exact sums by two-sum,
+// exact products by Veltkamp's split), so that each rounds to the double
+// nearest its value; series summed in plain doubles were up to 3 ulp off.
+struct CxDD {
+    double hi, lo;
+};
+constexpr CxDD cx_two_sum(double a, double b) {
+    const double s = a + b, bb = s - a;
+    return CxDD{s, (a - (s - bb)) + (b - bb)};
+}
+constexpr CxDD cx_two_prod(double a, double b) {
+    const double p = a * b;
+    const double ca = 134217729.0 * a, ah = ca - (ca - a), al = a - ah;   // 2^27 + 1
+    const double cb = 134217729.0 * b, bh = cb - (cb - b), bl = b - bh;
+    return CxDD{p, ((ah * bh - p) + ah * bl + al * bh) + al * bl};
+}
+constexpr CxDD cx_add(CxDD x, CxDD y) {
+    const CxDD s = cx_two_sum(x.hi, y.hi);
+    return cx_two_sum(s.hi, s.lo + x.lo + y.lo);
+}
+constexpr CxDD cx_mul(CxDD x, CxDD y) {
+    const CxDD p = cx_two_prod(x.hi, y.hi);
+    return cx_two_sum(p.hi, p.lo + (x.hi * y.lo + x.lo * y.hi));
+}
+constexpr CxDD cx_div(CxDD x, double d) {   // x / d
+    const double q1 = x.hi / d;
+    const CxDD p = cx_two_prod(q1, d);
+    const CxDD r = cx_two_sum(x.hi, -p.hi);
+    const double q2 = ((r.hi + r.lo) - p.lo + x.lo) / d;
+    return cx_two_sum(q1, q2);
+}
+// ln(1 + j/256) = 2 atanh(y), y = j / (512 + j) < 1/3
+constexpr double cx_ln_ratio(int j) {
+    const CxDD y = cx_div(CxDD{(double)j, 0.0}, 512.0 + j), y2 = cx_mul(y, y);
+    CxDD term = y, sum{0.0, 0.0};
+    for (int k = 0; k < 36; ++k) {
+        sum = cx_add(sum, cx_div(term, 2.0 * k + 1.0));
+        term = cx_mul(term, y2);
+    }
+    return 2.0 * sum.hi + 2.0 * sum.lo;
+}
 struct CxPair {
     double s, c;
 };
-// ln(1 + j/256) = 2 atanh(y), y = j / (512 + j) < 1/3
-constexpr double cx_ln_ratio(int j) {
-    const double y = (double)j / (512.0 + j), y2 = y * y;
-    double term = y, sum = 0.0;
-    for (int k = 0; k < 24; ++k) {
-        sum += term / (2 * k + 1);
-        term *= y2;
+// sin(pi a/256), cos(pi a/256) by their Taylor series, 0 <= a <= 64
+constexpr CxPair cx_sincos(int a) {
+    const CxDD pi{3.141592653589793, 1.2246467991473532e-16};
+    const CxDD x = cx_div(cx_mul(pi, CxDD{(double)a, 0.0}), 256.0);
+    const CxDD mx2 = cx_mul(x, CxDD{-x.hi, -x.lo});
+    CxDD ts = x, tc{1.0, 0.0}, s{0.0, 0.0}, c{0.0, 0.0};
+    for (int k = 0; k < 16; ++k) {
+        s = cx_add(s, ts);
+        c = cx_add(c, tc);
+        ts = cx_div(cx_mul(ts, mx2), (2.0 * k + 2.0) * (2.0 * k + 3.0));
+        tc = cx_div(cx_mul(tc, mx2), (2.0 * k + 1.0) * (2.0 * k + 2.0));
     }
-    return 2.0 * sum;
-}
-// sin x, cos x by their Taylor series, |x| <= pi/4
-constexpr CxPair cx_sincos(double x) {
-    double ts = x, tc = 1.0, s = 0.0, c = 0.0;
-    for (int k = 0; k < 14; ++k) {
-        s += ts;
-        c += tc;
-        ts *= -x * x / ((2.0 * k + 2.0) * (2.0 * k + 3.0));
-        tc *= -x * x / ((2.0 * k + 1.0) * (2.0 * k + 2.0));
-    }
-    return CxPair{s, c};
+    return CxPair{s.hi + s.lo, c.hi + c.lo};
 }
 constexpr F64Tabs cx_f64_tabs() {
     F64Tabs t{};
-    const double q = 3.141592653589793 / 256.0;
     for (int j = 0; j < 256; ++j) {
         t.lnm[j] = cx_ln_ratio(j);
         t.invm[j] = 256.0 / (256.0 + j);
         // reduce to [0, pi/4]: sin(pi - x) = sin x, cos(pi - x) = -cos x;
         // sin(pi/2 - x) = cos x, cos(pi/2 - x) = sin x
         const int a = j > 128 ? 256 - j : j;
-        const CxPair p = a <= 64 ? cx_sincos(a * q) : cx_sincos((128 - a) * q);
+        const CxPair p = a <= 64 ? cx_sincos(a) : cx_sincos(128 - a);
         t.sn[j] = a <= 64 ? p.s : p.c;
         const double c = a <= 64 ? p.c : p.s;
         t.cs[j] = j > 128 ? -c : c;
@@ -128,34 +164,51 @@ constexpr F64Tabs cx_f64_tabs() {
 }
 static __device__ const F64Tabs kF64Tabs = cx_f64_tabs();
 
-// ln x for x in (0, 1): x = m 2^e, m in [1, 2); the top 8 bits of m give the
-// breakpoint m_j = 1 + j/256, and ln m = ln m_j + ln(1 + t), t = (m - m_j)/m_j
-// in [0, 1/256), by its series to t^7 (the next term is below 3e-20)
-__device__ __forceinline__ double ln_uniform(double x) {
-    const long long b = __double_as_longlong(x);
-    const int e = (int)(b >> 52) - 1023;
-    const int j = (int)((b >> 44) & 0xff);
-    const double m = __longlong_as_double((b & 0x000fffffffffffffll) | 0x3ff0000000000000ll);
-    const double mj = __longlong_as_double((b & 0x000ff00000000000ll) | 0x3ff0000000000000ll);
+// ln U of the uniform U = (w + 1/2) 2^-32 = v 2^-33, v = 2w + 1 (odd, 33
+// bits), from the word itself: v = m 2^p with m in [1, 2) (p from the
+// leading zeros, m's mantissa bits by a shift), so U = m 2^(p - 33); the
+// top 8 bits of m give the breakpoint m_j = 1 + j/256, and
+// ln m = ln m_j + ln(1 + t), t = (m - m_j)/m_j in [0, 1/256), by its series
+// to t^6 (the next term is below 2e-18)
+__device__ __forceinline__ double ln_word(uint32_t w) {
+    const unsigned long long v = 2ull * w + 1ull;
+    const int p = 63 - __clzll((long long)v);                                  // 0 .. 32
+    const long long mb = (long long)((v << (52 - p)) & 0x000fffffffffffffull);  // mantissa bits of m
+    const int j = (int)(mb >> 44);
+    const double m = __longlong_as_double(mb | 0x3ff0000000000000ll);
+    const double mj = __longlong_as_double((mb & 0x000ff00000000000ll) | 0x3ff0000000000000ll);
     const double t = (m - mj) * __ldg(&kF64Tabs.invm[j]);   // m - m_j is exact
-    const double p =
-        t * fma(t, fma(t, fma(t, fma(t, fma(t, fma(t, 1.0 / 7.0, -1.0 / 6.0), 0.2), -0.25), 1.0 / 3.0), -0.5), 1.0);
-    return fma((double)e, 0.6931471805599453, __ldg(&kF64Tabs.lnm[j]) + p);
+    const double q = t * fma(t, fma(t, fma(t, fma(t, fma(t, -1.0 / 6.0, 0.2), -0.25), 1.0 / 3.0), -0.5), 1.0);
+    return fma((double)(p - 33), 0.6931471805599453, __ldg(&kF64Tabs.lnm[j]) + q);
 }
 
-// sin(pi u), cos(pi u) for u in [0, 1): u = j/256 + d with d in [0, 1/256)
-// exact, the table at j/256 and the series of x = pi d (<= 0.0123) to x^7
-// (sin) and x^6 (cos), the next terms being below 2e-20
-__device__ __forceinline__ void sincospi_uniform(double u, double* s, double* c) {
-    int j = (int)(u * 256.0);
-    j = j < 0 ? 0 : (j > 255 ? 255 : j);
-    const double d = fma((double)-j, 1.0 / 256.0, u);
-    const double x = d * 3.141592653589793, x2 = x * x;
-    const double sd = x * fma(x2, fma(x2, fma(x2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), 1.0);
+// sin(pi u), cos(pi u) for u = j/256 + x/pi, j the breakpoint and x in
+// [0, pi/256): the table at j/256 and the series of x (<= 0.0123) to x^5
+// (sin) and x^6 (cos), the next terms being below 1e-17 and 2e-20
+__device__ __forceinline__ void sincospi_tab(int j, double x, double* s, double* c) {
+    const double x2 = x * x;
+    const double sd = x * fma(x2, fma(x2, 1.0 / 120.0, -1.0 / 6.0), 1.0);
     const double cd = fma(x2, fma(x2, fma(x2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
     const double S = __ldg(&kF64Tabs.sn[j]), C = __ldg(&kF64Tabs.cs[j]);
     *s = fma(S, cd, C * sd);
     *c = fma(C, cd, -S * sd);
+}
+
+// ... of the uniform u = (w + 1/2) 2^-32 from the word: j is its top 8 bits
+// and x = pi (w mod 2^24 + 1/2) 2^-32, built as the double
+// 1 + (w mod 2^24 + 1/2) 2^-24 less 1 (exact) times pi/256 -- the same x,
+// bit for bit, as pi (u - j/256)
+__device__ __forceinline__ void sincospi_word(uint32_t w, double* s, double* c) {
+    const double r = __hiloint2double(0x3ff00000 | (int)((w & 0xffffffu) >> 4), (int)((w << 28) | 0x8000000u)) - 1.0;
+    sincospi_tab((int)(w >> 24), r * (3.141592653589793 / 256.0), s, c);
+}
+
+// ... of a uniform u in [0, 1) given as a double (the adjoint's stored
+// azimuth uniforms): u = j/256 + d with d exact, x = pi d
+__device__ __forceinline__ void sincospi_uniform(double u, double* s, double* c) {
+    int j = (int)(u * 256.0);
+    j = j < 0 ? 0 : (j > 255 ? 255 : j);
+    sincospi_tab(j, fma((double)-j, 1.0 / 256.0, u) * 3.141592653589793, s, c);
 }
 
 template <>
@@ -168,10 +221,13 @@ struct Ops<double> {
     }
     static __device__ __forceinline__ double unit_c(uint32_t u) { return unit(~u); }
     static __device__ __forceinline__ double ln(double x) { return log(x); }
-    // the step's uniform and the azimuth's: table driven (ln_uniform,
-    // sincospi_uniform above), 12% and 10% of the small FP64 configuration's
-    // time with CUDA's log and sincospi
-    static __device__ __forceinline__ double ln_step(double x) { return ln_uniform(x); }
+    // the step's uniform and the azimuth's, from their Philox words: table
+    // driven (ln_word, sincospi_word above); CUDA's log and sincospi took
+    // 12% and 10% of the small FP64 configuration's time
+    static __device__ __forceinline__ double ln_step_word(uint32_t w) { return ln_word(w); }
+    static __device__ __forceinline__ void sincos_pi_word(uint32_t w, double* s, double* c) {
+        sincospi_word(w, s, c);
+    }
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
     static __device__ __forceinline__ double rsqrt_(double x) { return rsqrt(x); }
     // 1/sqrt(x) for the squared norm x = 1 + e of a rotated unit vector: the
@@ -401,7 +457,7 @@ __device__ __forceinline__ void lane_lose(Lane<T>& L, const C& c, T W) {
 //     y' = y cos(phi) - x sin(phi),
 // the rotation q p q* written out (equal to it within rounding).
 template <class T, class C>
-__device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_phi) {
+__device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, uint32_t w_phi) {
     // sin(theta) = 2 sin(theta/2) cos(theta/2); FP64 takes it as
     // 2 sqrt(s2 (1 - s2)), one square root on the narrow FP64 unit, while
     // FP32 keeps the two roots (one root measured no faster there)
@@ -409,7 +465,7 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, T u_ph
     if constexpr (sizeof(T) == 8) sth = (T)2 * Ops<T>::sqrt_(s2 * ((T)1 - s2));
     else sth = (T)2 * Ops<T>::sqrt_(s2) * Ops<T>::sqrt_((T)1 - s2);
     T sp, cp;
-    Ops<T>::sincos_pi(u_phi, &sp, &cp);
+    Ops<T>::sincos_pi_word(w_phi, &sp, &cp);
     if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
     const T cth = (T)1 - (T)2 * s2;
     const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
@@ -606,7 +662,7 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     // steps with mean free path xip_g and marks the electron diffracting
     const bool diff_ev = ch == MCD_CH_DIFF;
     L.flags = diff_ev ? (L.flags | F_DIFFRACTING) : (L.flags & ~F_DIFFRACTING);
-    const T s = -Ops<T>::ln_step(Ops<T>::unit(r.y)) * (diff_ev ? c.xip : inv_tot);
+    const T s = -Ops<T>::ln_step_word(r.y) * (diff_ev ? c.xip : inv_tot);
     const T x0 = L.x, y0 = L.y, z0 = L.z;
     lane_move(L, c, s);
     // --- energy loss and polar angle (MC/tools/scattering.py:568-679)
@@ -649,7 +705,7 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     }
     const bool left = L.outcome != MCD_OUT_NONE;
     if (!left || (c.bits & MCD_Q_CROSSING_STEP)) lane_lose(L, c, W);
-    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
+    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, r.w);
     return ch;
 }
 
@@ -682,7 +738,7 @@ template <class T, bool REC, class C>
 __device__ __forceinline__ int cont_event_r(Lane<T>& L, const C& c, const uint4 r, EventOut<T>* ev) {
     const T E = L.E;
     const T sR = sig_ruth<T>(c, E);
-    const T s = -Ops<T>::ln_step(Ops<T>::unit(r.y)) * Ops<T>::div((T)1, sR);
+    const T s = -Ops<T>::ln_step_word(r.y) * Ops<T>::div((T)1, sR);
     if (!(s < (T)1e4)) {
         L.flags |= F_LONG_PATH;
         L.lpath_n += 1;
@@ -718,7 +774,7 @@ __device__ __forceinline__ int cont_event_r(Lane<T>& L, const C& c, const uint4 
     }
     const bool left = L.outcome != MCD_OUT_NONE;
     if (!left || (c.bits & MCD_Q_CROSSING_STEP)) lane_lose(L, c, dE);
-    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, uphi);
+    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, r.w);
     return MCD_CH_RUTH;
 }
 
