@@ -203,6 +203,25 @@ __device__ __forceinline__ void sincospi_word(uint32_t w, double* s, double* c) 
     sincospi_tab((int)(w >> 24), r * (3.141592653589793 / 256.0), s, c);
 }
 
+// cos(2 pi u), sin(2 pi u) of the uniform u = (w + 1/2) 2^-32 from the word:
+// 2u = k/256 + x/pi with k the top 9 bits of w; for k >= 256 (u >= 1/2)
+// the angle is pi more, which flips both signs; j = k mod 256 indexes the
+// table and x = pi (w mod 2^23 + 1/2) 2^-31, built from the low 23 bits as
+// sincospi_word builds its remainder
+__device__ __forceinline__ void cossin2pi_word(uint32_t w, double* c, double* s) {
+    const double r = __hiloint2double(0x3ff00000 | (int)((w & 0x7fffffu) >> 3), (int)((w << 29) | 0x10000000u)) - 1.0;
+    double sv, cv;
+    sincospi_tab((int)((w >> 23) & 0xffu), r * (3.141592653589793 / 256.0), &sv, &cv);
+    const int flip = (int)(w & 0x80000000u);   // the sign bit, flipped in the high words
+    *s = __hiloint2double(__double2hiint(sv) ^ flip, __double2loint(sv));
+    *c = __hiloint2double(__double2hiint(cv) ^ flip, __double2loint(cv));
+}
+
+// |x| by clearing the sign bit (an integer operation, not an FP64 one)
+__device__ __forceinline__ double abs_bits(double x) {
+    return __hiloint2double(__double2hiint(x) & 0x7fffffff, __double2loint(x));
+}
+
 // ... of a uniform u in [0, 1) given as a double (the adjoint's stored
 // azimuth uniforms): u = j/256 + d with d exact, x = pi d
 __device__ __forceinline__ void sincospi_uniform(double u, double* s, double* c) {
@@ -464,11 +483,23 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, uint32
     T sth;
     if constexpr (sizeof(T) == 8) sth = (T)2 * Ops<T>::sqrt_(s2 * ((T)1 - s2));
     else sth = (T)2 * Ops<T>::sqrt_(s2) * Ops<T>::sqrt_((T)1 - s2);
-    T sp, cp;
-    Ops<T>::sincos_pi_word(w_phi, &sp, &cp);
-    if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
+    // phi = 2 halfPhi, halfPhi = pi U (MC/tools/scattering.py:676); with
+    // the reference's fold cos(halfPhi) = +sqrt(1 - sin^2) (sin(halfPhi) >= 0)
+    // sin(phi) = 2 sin(halfPhi) |cos(halfPhi)| = |sin(2 pi U)|.  FP32 takes
+    // the double angle of sin/cos(pi U); FP64 reads cos/sin(2 pi U) from the
+    // table directly, four FP64 instructions fewer
+    T cph, sph;
+    if constexpr (sizeof(T) == 8) {
+        cossin2pi_word(w_phi, &cph, &sph);
+        if (c.bits & MCD_Q_HALF_PHI_FOLD) sph = abs_bits(sph);
+    } else {
+        T sp, cp;
+        Ops<T>::sincos_pi_word(w_phi, &sp, &cp);
+        if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
+        cph = (T)1 - (T)2 * sp * sp;
+        sph = (T)2 * sp * cp;
+    }
     const T cth = (T)1 - (T)2 * s2;
-    const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
     const T xx = L.yy * L.dz - L.yz * L.dy;
     const T xy = L.yz * L.dx - L.yx * L.dz;
     const T xz = L.yx * L.dy - L.yy * L.dx;
@@ -704,7 +735,10 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
         ev->ch = ch;
     }
     const bool left = L.outcome != MCD_OUT_NONE;
-    if (!left || (c.bits & MCD_Q_CROSSING_STEP)) lane_lose(L, c, W);
+    // a zero loss (Rutherford, diffraction) leaves E, and with it E > Emin,
+    // as it is: FP64 skips the update, an FP64 subtraction and comparison
+    const bool zero_loss = sizeof(T) == 8 && (ch == MCD_CH_RUTH || diff_ev);
+    if (!zero_loss && (!left || (c.bits & MCD_Q_CROSSING_STEP))) lane_lose(L, c, W);
     if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, r.w);
     return ch;
 }

@@ -1,5 +1,6 @@
-"""The FP64 transport's table-driven logarithm and sin/cos(pi U) of its
-uniforms U = (w + 1/2) 2^-32 (mcd_device.cuh: ln_word, sincospi_word), run on
+"""The FP64 transport's table-driven logarithm, sin/cos(pi U) and
+cos/sin(2 pi U) of its uniforms U = (w + 1/2) 2^-32 (mcd_device.cuh: ln_word,
+sincospi_word, cossin2pi_word), run on
 the GPU through a test kernel (tests/special_check.cu, compiled here), against
 the host: at 40 significant digits (Python's decimal) on 4000 words including
 the edge words and every breakpoint, and against numpy's libm on 2e6 seeded
@@ -35,7 +36,7 @@ def special(tmp_path_factory):
 
     def run(words):
         w = np.ascontiguousarray(words, dtype=np.uint32)
-        out = np.empty((w.size, 3), dtype=np.float64)
+        out = np.empty((w.size, 5), dtype=np.float64)
         assert lib.special_eval(w.ctypes.data, w.size, out.ctypes.data) == 0
         assert not np.isnan(out).any(), "the adjoint's sin/cos of the same uniform differs"
         return out
@@ -55,17 +56,21 @@ def edge_words():
 def decimal_ref(words):
     ctx = decimal.Context(prec=40)
     pi = decimal.Decimal("3.141592653589793238462643383279502884197169")
-    out = np.empty((len(words), 3))
-    for k, w in enumerate(words):
-        U = (decimal.Decimal(int(w)) + decimal.Decimal("0.5")) / decimal.Decimal(2 ** 32)
-        x = ctx.multiply(pi, U)
+    def sincos(x):
         x2 = ctx.multiply(x, x)
         s, c, ts, tc = decimal.Decimal(0), decimal.Decimal(0), x, decimal.Decimal(1)
-        for n in range(40):
+        for n in range(60):
             s, c = ctx.add(s, ts), ctx.add(c, tc)
             ts = ctx.divide(ctx.multiply(-ts, x2), (2 * n + 2) * (2 * n + 3))
             tc = ctx.divide(ctx.multiply(-tc, x2), (2 * n + 1) * (2 * n + 2))
-        out[k] = (float(U.ln(ctx)), float(s), float(c))
+        return s, c
+
+    out = np.empty((len(words), 5))
+    for k, w in enumerate(words):
+        U = (decimal.Decimal(int(w)) + decimal.Decimal("0.5")) / decimal.Decimal(2 ** 32)
+        s, c = sincos(ctx.multiply(pi, U))
+        s2, c2 = sincos(ctx.multiply(pi, ctx.multiply(2, U) - 1))       # 2 pi U = pi + pi (2U - 1)
+        out[k] = (float(U.ln(ctx)), float(s), float(c), float(-c2), float(-s2))
     return out
 
 
@@ -91,3 +96,5 @@ def test_against_libm_on_two_million_words(special):
     # the slope) besides its own
     assert np.abs(got[:, 1] - np.sin(np.pi * U)).max() <= 1e-15
     assert np.abs(got[:, 2] - np.cos(np.pi * U)).max() <= 1e-15
+    assert np.abs(got[:, 3] - np.cos(2 * np.pi * U)).max() <= 2e-15
+    assert np.abs(got[:, 4] - np.sin(2 * np.pi * U)).max() <= 2e-15
