@@ -478,7 +478,7 @@ __device__ __forceinline__ void lane_lose(Lane<T>& L, const C& c, T W) {
 template <class T, class C>
 __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, uint32_t w_phi) {
     // sin(theta) = 2 sin(theta/2) cos(theta/2); FP64 takes it as
-    // 2 sqrt(s2 (1 - s2)), one square root on the narrow FP64 unit, while
+    // 2 sqrt(s2 (1 - s2)), one FP64 square root instead of two, while
     // FP32 keeps the two roots (one root measured no faster there)
     T sth;
     if constexpr (sizeof(T) == 8) sth = (T)2 * Ops<T>::sqrt_(s2 * ((T)1 - s2));
@@ -572,9 +572,9 @@ __device__ __forceinline__ int tab_pick(const C& c, float E, float U, float* Eto
 // layout at kSig64Cells): the octave from the exponent bits of E, the cell
 // from the top mantissa bits and its offset f from the other 44 (exact, by
 // integer operations and one subtraction), then each column read is three
-// FMAs.  The FP64 unit is narrow on this GPU and busy for the whole warp
-// however few lanes are active, so the lookup is built to issue few FP64
-// instructions: no logarithm, no interpolation weights, no division.  With
+// FMAs.  A small FP64 run is a chain of dependent instructions in which the
+// FP64 ones take longest, so the lookup is built to issue few of them: no
+// logarithm, no interpolation weights, no division.  With
 // diffraction (a constant cross section dS) the total grows by the factor
 // g = 1 + dS lambda; the event diffracts when U g > 1, otherwise U g is
 // compared with the fractions of the other channels.  Returns -1 for a cell

@@ -546,12 +546,11 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
         // trajectories are latency chains, and an SM with fewer lanes runs
         // each chain faster (1000 FP32 electrons: 1.00 ms in 32 blocks of 32,
         // 0.82 ms in 125 blocks of 8).  FP64 goes further, down to 2 threads
-        // while the grid stays within one warp per scheduler (4 per SM): an
-        // FP64 instruction occupies its scheduler's narrow FP64 unit for the
-        // whole warp however few lanes are active, so electrons spread over
-        // more schedulers finish sooner (1000 FP64 electrons with their
-        // table: 7.37 ms in blocks of 8, 6.69 ms in blocks of 2, 8.70 ms in
-        // blocks of 1, where schedulers hold two warps)
+        // while the grid stays within one warp per scheduler (4 per SM):
+        // fewer lanes per warp diverge less, and the longest FP64 chain
+        // shares its scheduler with no other warp (1000 FP64 electrons with
+        // their table: 7.37 ms in blocks of 8, 6.69 ms in blocks of 2,
+        // 8.70 ms in blocks of 1, where schedulers hold two warps)
         block_size = 128;
         int dev = 0, sms = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
