@@ -475,30 +475,34 @@ __device__ __forceinline__ void lane_lose(Lane<T>& L, const C& c, T W) {
 //     d' = d cos(theta) + sin(theta) (x cos(phi) + y sin(phi)),
 //     y' = y cos(phi) - x sin(phi),
 // the rotation q p q* written out (equal to it within rounding).
+// cos(phi), sin(phi) of the event's azimuth from its Philox word: phi =
+// 2 halfPhi, halfPhi = pi U (MC/tools/scattering.py:676); with the
+// reference's fold cos(halfPhi) = +sqrt(1 - sin^2) (sin(halfPhi) >= 0)
+// sin(phi) = 2 sin(halfPhi) |cos(halfPhi)| = |sin(2 pi U)|.  FP32 takes the
+// double angle of sin/cos(pi U); FP64 reads cos/sin(2 pi U) from the table
+// directly, four FP64 instructions fewer.
 template <class T, class C>
-__device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, uint32_t w_phi) {
+__device__ __forceinline__ void azimuth(const C& c, uint32_t w_phi, T* cph, T* sph) {
+    if constexpr (sizeof(T) == 8) {
+        cossin2pi_word(w_phi, cph, sph);
+        if (c.bits & MCD_Q_HALF_PHI_FOLD) *sph = abs_bits(*sph);
+    } else {
+        T sp, cp;
+        Ops<T>::sincos_pi_word(w_phi, &sp, &cp);
+        if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
+        *cph = (T)1 - (T)2 * sp * sp;
+        *sph = (T)2 * sp * cp;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void lane_rotate_cs(Lane<T>& L, T s2, T cph, T sph) {
     // sin(theta) = 2 sin(theta/2) cos(theta/2); FP64 takes it as
     // 2 sqrt(s2 (1 - s2)), one FP64 square root instead of two, while
     // FP32 keeps the two roots (one root measured no faster there)
     T sth;
     if constexpr (sizeof(T) == 8) sth = (T)2 * Ops<T>::sqrt_(s2 * ((T)1 - s2));
     else sth = (T)2 * Ops<T>::sqrt_(s2) * Ops<T>::sqrt_((T)1 - s2);
-    // phi = 2 halfPhi, halfPhi = pi U (MC/tools/scattering.py:676); with
-    // the reference's fold cos(halfPhi) = +sqrt(1 - sin^2) (sin(halfPhi) >= 0)
-    // sin(phi) = 2 sin(halfPhi) |cos(halfPhi)| = |sin(2 pi U)|.  FP32 takes
-    // the double angle of sin/cos(pi U); FP64 reads cos/sin(2 pi U) from the
-    // table directly, four FP64 instructions fewer
-    T cph, sph;
-    if constexpr (sizeof(T) == 8) {
-        cossin2pi_word(w_phi, &cph, &sph);
-        if (c.bits & MCD_Q_HALF_PHI_FOLD) sph = abs_bits(sph);
-    } else {
-        T sp, cp;
-        Ops<T>::sincos_pi_word(w_phi, &sp, &cp);
-        if (c.bits & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
-        cph = (T)1 - (T)2 * sp * sp;
-        sph = (T)2 * sp * cp;
-    }
     const T cth = (T)1 - (T)2 * s2;
     const T xx = L.yy * L.dz - L.yz * L.dy;
     const T xy = L.yz * L.dx - L.yx * L.dz;
@@ -519,6 +523,13 @@ __device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, uint32
     L.yx = ny[0] * ry;
     L.yy = ny[1] * ry;
     L.yz = ny[2] * ry;
+}
+
+template <class T, class C>
+__device__ __forceinline__ void lane_rotate(Lane<T>& L, const C& c, T s2, uint32_t w_phi) {
+    T cph, sph;
+    azimuth<T>(c, w_phi, &cph, &sph);
+    lane_rotate_cs(L, s2, cph, sph);
 }
 
 // ---------------------------------------------------------------------------
@@ -641,6 +652,10 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     const T E = L.E;
     int ch = MCD_CH_QUINN;
     T inv_tot;
+    // FP64: the azimuth's cos/sin depend on the word alone; computed first,
+    // their FP64 chain overlaps the channel pick's instead of closing the event
+    T cph = (T)0, sph = (T)0;
+    if constexpr (sizeof(T) == 8) azimuth<T>(c, r.w, &cph, &sph);
     if (use_tab) {
         if constexpr (sizeof(T) == 4) {
             float Etot;
@@ -739,7 +754,10 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     // as it is: FP64 skips the update, an FP64 subtraction and comparison
     const bool zero_loss = sizeof(T) == 8 && (ch == MCD_CH_RUTH || diff_ev);
     if (!zero_loss && (!left || (c.bits & MCD_Q_CROSSING_STEP))) lane_lose(L, c, W);
-    if (L.outcome == MCD_OUT_NONE) lane_rotate(L, c, s2, r.w);
+    if (L.outcome == MCD_OUT_NONE) {
+        if constexpr (sizeof(T) == 8) lane_rotate_cs(L, s2, cph, sph);
+        else lane_rotate(L, c, s2, r.w);
+    }
     return ch;
 }
 
