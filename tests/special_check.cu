@@ -1,7 +1,7 @@
-// Test kernel of the GPU tests (not part of the library): evaluates the FP64
+// Test kernels of the GPU tests (not part of the library): evaluate the FP64
 // transport's table-driven logarithm, sin/cos(pi u) and cos/sin(2 pi u) of
 // Philox words, as the transport calls them, for comparison with 40-digit
-// values and the host's libm.
+// values and the host's libm, and its Newton-Raphson reciprocal.
 #include <cstdint>
 
 #include "mcd_device.cuh"
@@ -22,6 +22,31 @@ __global__ void k_special(const uint32_t* w, int64_t n, double* out) {
     if (s2 != s || c2 != c) out[5 * i + 1] = __longlong_as_double(0x7ff8000000000000ll);
 }
 }  // namespace
+
+static __global__ void k_rcp(const double* d, int64_t n, double* out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = mcd::rcp_pos(d[i]);
+}
+
+// d (host, n, positive normal) -> out (host, n): the FP64 transport's 1/d
+extern "C" int rcp_eval(const double* d, int64_t n, double* out) {
+    double *dd = nullptr, *dout = nullptr;
+    if (cudaMalloc(&dd, n * sizeof(double)) != cudaSuccess) return 1;
+    if (cudaMalloc(&dout, n * sizeof(double)) != cudaSuccess) {
+        cudaFree(dd);
+        return 1;
+    }
+    int rc = 0;
+    if (cudaMemcpy(dd, d, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) rc = 2;
+    if (!rc) {
+        k_rcp<<<(unsigned)((n + 255) / 256), 256>>>(dd, n, dout);
+        if (cudaGetLastError() != cudaSuccess) rc = 3;
+    }
+    if (!rc && cudaMemcpy(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = 4;
+    cudaFree(dd);
+    cudaFree(dout);
+    return rc;
+}
 
 // words (host, n) -> out (host, 5 n: ln U, sin pi U, cos pi U, cos 2 pi U,
 // sin 2 pi U); 0 on success

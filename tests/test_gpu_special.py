@@ -33,6 +33,8 @@ def special(tmp_path_factory):
     lib = C.CDLL(so)
     lib.special_eval.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
     lib.special_eval.restype = C.c_int
+    lib.rcp_eval.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
+    lib.rcp_eval.restype = C.c_int
 
     def run(words):
         w = np.ascontiguousarray(words, dtype=np.uint32)
@@ -40,6 +42,13 @@ def special(tmp_path_factory):
         assert lib.special_eval(w.ctypes.data, w.size, out.ctypes.data) == 0
         assert not np.isnan(out).any(), "the adjoint's sin/cos of the same uniform differs"
         return out
+
+    def rcp(d):
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        out = np.empty_like(d)
+        assert lib.rcp_eval(d.ctypes.data, d.size, out.ctypes.data) == 0
+        return out
+    run.rcp = rcp
     return run
 
 
@@ -98,3 +107,17 @@ def test_against_libm_on_two_million_words(special):
     assert np.abs(got[:, 2] - np.cos(np.pi * U)).max() <= 1e-15
     assert np.abs(got[:, 3] - np.cos(2 * np.pi * U)).max() <= 2e-15
     assert np.abs(got[:, 4] - np.sin(2 * np.pi * U)).max() <= 2e-15
+
+
+def test_reciprocal_within_two_ulp(special):
+    """rcp_pos (the Rutherford angle's 1/(E (1 - U) + a0)): the hardware
+    approximation and two third-order Newton-Raphson steps, within two ulp
+    of the IEEE quotient over 1e-3 .. 1e7 (log-uniform, 1e6 values) and at
+    every power of two in that range and its neighbours."""
+    rng = np.random.default_rng(7)
+    d = np.exp(rng.uniform(np.log(1e-3), np.log(1e7), 1_000_000))
+    p2 = 2.0 ** np.arange(-9, 24)
+    d = np.concatenate([d, p2, np.nextafter(p2, 0.0), np.nextafter(p2, np.inf)])
+    got, want = special.rcp(d), 1.0 / d
+    ulp = np.spacing(want)
+    assert np.all(np.abs(got - want) <= 2 * ulp), np.max(np.abs(got - want) / ulp)
