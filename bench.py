@@ -958,7 +958,7 @@ def run_mcd(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--steps", type=int, default=12)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mcd", choices=("mcd", "reference"))
     ap.add_argument("--block", type=int, default=0, help="batched block size (0: autotune)")
