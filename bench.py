@@ -52,15 +52,15 @@ CPU_SAMPLE_ELECTRONS = 40000
 BATCHED_DRAM_BYTES = 55.48e6 + 0.47e6
 # warp instructions issued per event by the batched kernel on this workload
 # in its tuned shape (two blocks of 576 per SM, 56 registers), from an ncu
-# capture of a quarter-size launch (2.0314e10 instructions for 1.3855e9
+# capture of a quarter-size launch (2.0065e10 instructions for 1.3855e9
 # events); the issue peak is one warp instruction per scheduler per cycle,
 # 4 schedulers per SM
-WARP_INST_PER_EVENT = 14.66
+WARP_INST_PER_EVENT = 14.48
 # the same capture's unit fractions (of peak sustained): issue-active cycles,
 # threads per warp instruction / 32, the L1/TEX unit, its shared-memory
 # wavefronts, and L2
-BATCHED_NCU = {"issue_active": 0.776, "warp_execution_efficiency": 0.706, "l1tex_throughput": 0.738,
-               "shared_wavefronts": 0.293, "l2_throughput": 0.029,
+BATCHED_NCU = {"issue_active": 0.770, "warp_execution_efficiency": 0.714, "l1tex_throughput": 0.747,
+               "shared_wavefronts": 0.301, "l2_throughput": 0.029,
                "capture": "ncu --set full of k_batched_lr (2 x 576, 56 registers) on a quarter of the workload "
                           "(1.3855e9 events)"}
 
