@@ -21,12 +21,12 @@ __global__ void k_special(const uint32_t* w, int64_t n, double* out) {
     mcd::sincospi_uniform(mcd::Ops<double>::unit(w[i]), &s2, &c2);
     if (s2 != s || c2 != c) out[5 * i + 1] = __longlong_as_double(0x7ff8000000000000ll);
 }
-}  // namespace
 
-static __global__ void k_rcp(const double* d, int64_t n, double* out) {
+__global__ void k_rcp(const double* d, int64_t n, double* out) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = mcd::rcp_pos(d[i]);
 }
+}  // namespace
 
 // d (host, n, positive normal) -> out (host, n): the FP64 transport's 1/d
 extern "C" int rcp_eval(const double* d, int64_t n, double* out) {
