@@ -270,8 +270,66 @@ __device__ __forceinline__ void depth_sweep(const C& c, const AdjBuf& buf, uint6
     *gn = sn;
 }
 
+// The backward pass runs only for backscattered electrons, a fraction of
+// the launch: each warp owns a range of kBwdRange electrons and hands its
+// backscattered ones to idle lanes in index order, so that warps stay full
+// (one thread per electron left about 5 of 32 lanes active).
+constexpr int kBwdRange = 256;
+
+struct BksFeed {
+    uint64_t pos, end;   // next electron of the range to scan, end of the range
+    uint64_t base;       // electron of bit 0 of `found`
+    unsigned found;      // backscattered electrons of [base, base + 32) not handed out yet
+};
+
+// Hands the next backscattered electrons (with a checkpointed sweep) to the
+// lanes in `idle`, lowest lane first; returns this lane's electron or -1.
+// Called by the whole warp with the same `idle` and `f`.
+__device__ __forceinline__ int64_t bks_take(BksFeed& f, const AdjBuf& buf, unsigned idle, int lane) {
+    int64_t mine = -1;
+    const unsigned lt = (1u << lane) - 1u;
+    while (idle) {
+        if (f.found == 0u) {
+            if (f.pos >= f.end) break;
+            const uint64_t j = f.pos + (uint64_t)lane;
+            bool b = false;
+            if (j < f.end) {
+                const int k = buf.kstar[j];
+                b = k > 0 && (k - 1) / kSeg < buf.max_ckpt;
+            }
+            f.found = __ballot_sync(0xffffffffu, b);
+            f.base = f.pos;
+            f.pos += 32;
+            continue;
+        }
+        const int give = min(__popc(f.found), __popc(idle));
+        const int r = __popc(idle & lt);   // this lane's rank among the idle ones
+        if (((idle >> lane) & 1u) && r < give) {
+            unsigned m = f.found;
+            for (int q = 0; q < r; ++q) m &= m - 1u;
+            mine = (int64_t)(f.base + (uint64_t)(__ffs(m) - 1));
+        }
+        for (int q = 0; q < give; ++q) {   // the handed-out electrons and the lanes that took them
+            f.found &= f.found - 1u;
+            idle &= idle - 1u;
+        }
+    }
+    return mine;
+}
+
+// d(loss)/d(exit quantity) of electron i: the soft-bin weights' derivative
+// plus the sum term
+template <class T>
+__device__ __forceinline__ double exit_adjoint(const SoftHist& sh, const AdjBuf& buf, const double* grad_h,
+                                               double inv_n, uint64_t i) {
+    const double q = (double)static_cast<const T*>(buf.E_exit)[i];
+    double g = grad_h[sh.nbins];
+    soft_bins(sh, q, [&](int b, double w, double d) { g += grad_h[b] * inv_n * (-d * sh.inv_s2) * w; });
+    return g;
+}
+
 template <class T, bool DEPTH>
-__global__ void __launch_bounds__(128) k_adj_bwd(const SimConst<T> cp, const SoftHist sh, const AdjBuf buf,
+__global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const SoftHist sh, const AdjBuf buf,
                                                  const double* grad_h, double inv_n, double inv_j,
                                                  double inv_ns, double* grad) {
     __shared__ SimConst<T> c;
@@ -281,63 +339,76 @@ __global__ void __launch_bounds__(128) k_adj_bwd(const SimConst<T> cp, const Sof
         red[0] = red[1] = 0.0;
     }
     __syncthreads();
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const uint64_t n = (uint64_t)c.num_el;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t lo = warp * (uint64_t)kBwdRange;
+    BksFeed f{lo < n ? lo : n, lo + kBwdRange < n ? lo + kBwdRange : n, 0, 0u};
+    const T* ck = static_cast<const T*>(buf.ckpt);
     double gj = 0.0, gn = 0.0;
-    if (DEPTH && i < (uint64_t)c.num_el) {
-        const int mstar = buf.kstar[i];
-        if (mstar > 0 && (mstar - 1) / kSeg < buf.max_ckpt) {
-            const double Z = (double)static_cast<const T*>(buf.E_exit)[i];
-            double g0 = grad_h[sh.nbins];
-            soft_bins(sh, Z, [&](int b, double w, double d) { g0 += grad_h[b] * inv_n * (-d * sh.inv_s2) * w; });
-            T sj, sn;
-            depth_sweep<T>(c, buf, i, c.first + i, mstar, (T)g0, (T)inv_j, (T)inv_ns, &sj, &sn);
-            gj = (double)sj;
-            gn = (double)sn;
-        }
-    } else if (!DEPTH && i < (uint64_t)c.num_el) {
-        const int kstar = buf.kstar[i];
-        if (kstar > 0 && (kstar - 1) / kSeg < buf.max_ckpt) {
-            const T* ck = static_cast<const T*>(buf.ckpt);
-            const size_t n = (size_t)c.num_el;
-            const uint64_t elec = c.first + i;
-            // lambda at the exit energy: derivative of the soft-bin weights + the sum
-            const double Ex = (double)static_cast<const T*>(buf.E_exit)[i];
-            double lam0 = grad_h[sh.nbins];
-            soft_bins(sh, Ex, [&](int b, double w, double d) { lam0 += grad_h[b] * inv_n * (-d * sh.inv_s2) * w; });
-            // the sweep runs in the transport precision: lambda is a product of
-            // factors 1 + O(1e-2) and each step adds one term to the sums
-            T lam = (T)lam0, sj = (T)0, sn = (T)0;
-            const T ij = (T)inv_j, ins = (T)inv_ns;
-            T Eseg[kSeg], sseg[kSeg];
-            for (int m = (kstar - 1) / kSeg; m >= 0; --m) {
-                const int k0 = m * kSeg;
-                const int len = min(kSeg, kstar - k0);
-                T E = ck[(size_t)m * n + i];
-                for (int j = 0; j < len; ++j) {   // recompute the segment exactly as the forward did
-                    const T s = step_len<T>(c, E, elec, k0 + j);
-                    Eseg[j] = E;
-                    sseg[j] = s;
-                    E = E - Ops<T>::mul_rn(s, stopping<T>(c, E));
-                }
-                for (int j = len - 1; j >= 0; --j) {   // reverse sweep
-                    const T Ek = Eseg[j], s = sseg[j];
-                    T S, SE, Sj;
-                    stopping_derivs<T>(c, Ek, &S, &SE, &Sj);
-                    sj += lam * (-s * Sj * ij);
-                    // ds/dn = -s/n and dS/dn = S/n: the two terms cancel
-                    sn += lam * (-((-s * ins) * S + s * (S * ins)));
-                    lam *= (T)1 + s * (dlnsig<T>(c, Ek) * S - SE);
-                }
+    // lane state: its electron, the exit event, the segment to sweep next and
+    // (exit energy) the adjoint of E and the electron's parameter sums
+    int64_t cur = -1;
+    int ks = 0, m = 0;
+    T lam = (T)0, sj = (T)0, sn = (T)0;
+    const T ij = (T)inv_j, ins = (T)inv_ns;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, cur < 0);
+        if (idle) {
+            const int64_t e = bks_take(f, buf, idle, lane);
+            if (e >= 0) {
+                cur = e;
+                ks = buf.kstar[e];
+                m = (ks - 1) / kSeg;
+                // the sweep runs in the transport precision: lambda is a
+                // product of factors 1 + O(1e-2) and each step adds one term
+                lam = (T)exit_adjoint<T>(sh, buf, grad_h, inv_n, (uint64_t)e);
+                sj = sn = (T)0;
             }
-            gj = (double)sj;
-            gn = (double)sn;
+        }
+        if (__ballot_sync(0xffffffffu, cur >= 0) == 0u) break;
+        if (cur < 0) continue;
+        const uint64_t i = (uint64_t)cur;
+        const uint64_t elec = c.first + i;
+        if constexpr (DEPTH) {   // the whole electron in one trip
+            T a, b;
+            depth_sweep<T>(c, buf, i, elec, ks, lam, ij, ins, &a, &b);
+            gj += (double)a;
+            gn += (double)b;
+            cur = -1;
+            continue;
+        }
+        // exit energy: one 64-event segment per trip, the last one first
+        const int k0 = m * kSeg;
+        const int len = min(kSeg, ks - k0);
+        T Eseg[kSeg], sseg[kSeg];
+        T E = ck[(size_t)m * n + i];
+        for (int j = 0; j < len; ++j) {   // recompute the segment exactly as the forward did
+            const T s = step_len<T>(c, E, elec, k0 + j);
+            Eseg[j] = E;
+            sseg[j] = s;
+            E = E - Ops<T>::mul_rn(s, stopping<T>(c, E));
+        }
+        for (int j = len - 1; j >= 0; --j) {   // reverse sweep
+            const T Ek = Eseg[j], s = sseg[j];
+            T S, SE, Sj;
+            stopping_derivs<T>(c, Ek, &S, &SE, &Sj);
+            sj += lam * (-s * Sj * ij);
+            // ds/dn = -s/n and dS/dn = S/n: the two terms cancel
+            sn += lam * (-((-s * ins) * S + s * (S * ins)));
+            lam *= (T)1 + s * (dlnsig<T>(c, Ek) * S - SE);
+        }
+        if (--m < 0) {
+            gj += (double)sj;
+            gn += (double)sn;
+            cur = -1;
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
         gj += __shfl_down_sync(0xffffffffu, gj, o);
         gn += __shfl_down_sync(0xffffffffu, gn, o);
     }
-    if ((threadIdx.x & 31) == 0) {
+    if (lane == 0) {
         atomicAdd(&red[0], gj);
         atomicAdd(&red[1], gn);
     }
@@ -447,7 +518,8 @@ extern "C" int mcd_adjoint(const mcd_sim* sim, const mcd_material* mat, const mc
     int rc = adj_args(sim, mat, hist, buf, &sh, &ab);
     if (rc != MCD_OK) return rc;
     if (!grad_hist || !grad) return MCD_EINVAL;
-    const unsigned long long grid = ((unsigned long long)sim->num_el + 127) / 128;
+    // one warp per kBwdRange electrons, four warps per block
+    const unsigned long long grid = ((unsigned long long)sim->num_el + 4 * kBwdRange - 1) / (4 * kBwdRange);
     if (grid == 0) return MCD_OK;
     if (grid > 0x7fffffffull) return MCD_ETOOBIG;
     const double inv_n = 1.0 / (double)sim->num_el;
