@@ -40,21 +40,33 @@ struct SoftHist {
     int32_t nbins;
     int32_t quantity;   // MCD_ADJ_EXIT_E or MCD_ADJ_MAX_DEPTH
     double lo, width, inv2s2, inv_s2;
+    double inv_width, reach;   // 1 / width; 8 sigma
+    // the same in FP32, for FP32 runs: their soft bins are evaluated in FP32
+    // (and summed in FP64), so that an FP32 run issues no FP64 arithmetic
+    // per electron -- the backward takes its electrons a few lanes at a time,
+    // and the FP64 unit charges each of those instructions in full
+    float f_lo, f_inv_width, f_width, f_inv2s2, f_inv_s2, f_reach;
 };
 
 constexpr int kDepthState = 8;   // E, z, d (3), y (3) per depth checkpoint
 
-// Gaussian soft bins within 8 sigma of E: calls f(bin, weight, d = E - c_b)
-template <class F>
-__device__ __forceinline__ void soft_bins(const SoftHist& sh, double E, F f) {
-    const double reach = 8.0 * rsqrt(2.0 * sh.inv2s2);
-    int b0 = (int)floor((E - reach - sh.lo) / sh.width - 0.5);
-    int b1 = (int)ceil((E + reach - sh.lo) / sh.width - 0.5);
+// Gaussian soft bins within 8 sigma of the quantity q, in the transport
+// precision T: calls f(bin, weight, d = q - c_b)
+template <class T, class F>
+__device__ __forceinline__ void soft_bins(const SoftHist& sh, T q, F f) {
+    T lo, w, iw, i2, reach;
+    if constexpr (sizeof(T) == 8) {
+        lo = sh.lo, w = sh.width, iw = sh.inv_width, i2 = sh.inv2s2, reach = sh.reach;
+    } else {
+        lo = sh.f_lo, w = sh.f_width, iw = sh.f_inv_width, i2 = sh.f_inv2s2, reach = sh.f_reach;
+    }
+    int b0 = (int)floor((q - reach - lo) * iw - (T)0.5);
+    int b1 = (int)ceil((q + reach - lo) * iw - (T)0.5);
     b0 = b0 < 0 ? 0 : b0;
     b1 = b1 > sh.nbins - 1 ? sh.nbins - 1 : b1;
     for (int b = b0; b <= b1; ++b) {
-        const double d = E - (sh.lo + (b + 0.5) * sh.width);
-        f(b, exp(-d * d * sh.inv2s2), d);
+        const T d = q - (lo + ((T)b + (T)0.5) * w);
+        f(b, exp(-d * d * i2), d);
     }
 }
 
@@ -145,9 +157,8 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
         const T q = depth ? L.max_z : L.E_row;
         static_cast<T*>(buf.E_exit)[i] = q;
         if (bks) {
-            const double E = (double)q;
-            soft_bins(sh, E, [&](int b, double w, double) { if (w > 0.0) atomicAdd(&sh_h[b], w); });
-            atomicAdd(&sh_h[sh.nbins], E);
+            soft_bins<T>(sh, q, [&](int b, T w, T) { if (w > (T)0) atomicAdd(&sh_h[b], (double)w); });
+            atomicAdd(&sh_h[sh.nbins], (double)q);
             atomicAdd(&sh_h[sh.nbins + 1], 1.0);
         }
         atomicAdd(&s_cnt[L.outcome & 7], 1ull);
@@ -318,13 +329,13 @@ __device__ __forceinline__ int64_t bks_take(BksFeed& f, const AdjBuf& buf, unsig
 }
 
 // d(loss)/d(exit quantity) of electron i: the soft-bin weights' derivative
-// plus the sum term
+// plus the sum term, in T, with gh[b] = dL/dh_b / N and gh[nbins] = dL/dsum
 template <class T>
-__device__ __forceinline__ double exit_adjoint(const SoftHist& sh, const AdjBuf& buf, const double* grad_h,
-                                               double inv_n, uint64_t i) {
-    const double q = (double)static_cast<const T*>(buf.E_exit)[i];
-    double g = grad_h[sh.nbins];
-    soft_bins(sh, q, [&](int b, double w, double d) { g += grad_h[b] * inv_n * (-d * sh.inv_s2) * w; });
+__device__ __forceinline__ T exit_adjoint(const SoftHist& sh, const AdjBuf& buf, const T* gh, uint64_t i) {
+    const T q = static_cast<const T*>(buf.E_exit)[i];
+    const T is2 = sizeof(T) == 8 ? (T)sh.inv_s2 : (T)sh.f_inv_s2;
+    T g = gh[sh.nbins];
+    soft_bins<T>(sh, q, [&](int b, T w, T d) { g += gh[b] * (-d * is2) * w; });
     return g;
 }
 
@@ -334,10 +345,12 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
                                                  double inv_ns, double* grad) {
     __shared__ SimConst<T> c;
     __shared__ double red[2];
+    __shared__ T gh[MCD_HIST_E_MAX + 1];
     if (threadIdx.x == 0) {
         c = cp;
         red[0] = red[1] = 0.0;
     }
+    for (int b = threadIdx.x; b <= sh.nbins; b += blockDim.x) gh[b] = (T)(b < sh.nbins ? grad_h[b] * inv_n : grad_h[b]);
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const uint64_t n = (uint64_t)c.num_el;
@@ -362,7 +375,7 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
                 m = (ks - 1) / kSeg;
                 // the sweep runs in the transport precision: lambda is a
                 // product of factors 1 + O(1e-2) and each step adds one term
-                lam = (T)exit_adjoint<T>(sh, buf, grad_h, inv_n, (uint64_t)e);
+                lam = exit_adjoint<T>(sh, buf, gh, (uint64_t)e);
                 sj = sn = (T)0;
             }
         }
@@ -434,7 +447,7 @@ __global__ void __launch_bounds__(256) k_adj_chain(const SimConst<T> cp, const S
         const int kstar = buf.kstar[i];
         if (kstar >= 0) {
             const uint64_t elec = c.first + i;
-            double Ed;
+            T Ed;
             if (sh.quantity == MCD_ADJ_MAX_DEPTH) {
                 // the forward's own events up to the deepest point
                 Lane<T> L;
@@ -443,17 +456,17 @@ __global__ void __launch_bounds__(256) k_adj_chain(const SimConst<T> cp, const S
                     EventOut<T> ev;
                     cont_event<T, false>(L, c, elec, &ev);
                 }
-                Ed = (double)L.z;
+                Ed = L.z;
             } else {
                 T E = c.E0;
                 for (int k = 0; k < kstar; ++k) {
                     const T s = step_len<T>(c, E, elec, k);
                     E = E - Ops<T>::mul_rn(s, stopping<T>(c, E));
                 }
-                Ed = (double)E;
+                Ed = E;
             }
-            soft_bins(sh, Ed, [&](int b, double w, double) { if (w > 0.0) atomicAdd(&sh_h[b], w); });
-            atomicAdd(&sh_h[sh.nbins], Ed);
+            soft_bins<T>(sh, Ed, [&](int b, T w, T) { if (w > (T)0) atomicAdd(&sh_h[b], (double)w); });
+            atomicAdd(&sh_h[sh.nbins], (double)Ed);
             atomicAdd(&sh_h[sh.nbins + 1], 1.0);
         }
     }
@@ -479,6 +492,14 @@ static int adj_args(const mcd_sim* sim, const mcd_material* mat, const mcd_softh
     sh->width = (hist->hi - hist->lo) / hist->nbins;
     sh->inv2s2 = 1.0 / (2.0 * hist->sigma * hist->sigma);
     sh->inv_s2 = 1.0 / (hist->sigma * hist->sigma);
+    sh->inv_width = 1.0 / sh->width;
+    sh->reach = 8.0 * hist->sigma;
+    sh->f_lo = (float)sh->lo;
+    sh->f_width = (float)sh->width;
+    sh->f_inv_width = (float)sh->inv_width;
+    sh->f_inv2s2 = (float)sh->inv2s2;
+    sh->f_inv_s2 = (float)sh->inv_s2;
+    sh->f_reach = (float)sh->reach;
     ab->ckpt = buf->ckpt;
     ab->kstar = buf->kstar;
     ab->E_exit = buf->E_exit;
