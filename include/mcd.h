@@ -380,6 +380,12 @@ typedef struct mcd_adjoint_buf {
                                 of the first outcome row, or deepest z)     */
     int32_t max_ckpt;
     int32_t reserved;
+    unsigned long long* queue;
+                             /* one device word (or NULL): the forward pass
+                                zeroes it on its stream and runs a resident
+                                grid whose lanes take the next electron from
+                                it as they finish; NULL runs one thread per
+                                electron instead                            */
 } mcd_adjoint_buf;
 
 /* Continuous-mode forward pass that also stores the adjoint checkpoints.

@@ -34,6 +34,7 @@ struct AdjBuf {
     int32_t* kstar;    // exit event of 'bks' electrons, -1 otherwise
     void* E_exit;      // T
     int32_t max_ckpt;
+    unsigned long long* queue;   // the forward pass's work queue, or nullptr
 };
 
 struct SoftHist {
@@ -102,9 +103,16 @@ __device__ __forceinline__ T dlnsig(const C& c, T E) {
     return rel - Ops<T>::div((T)1, E + c.aS);
 }
 
+// The forward pass: every electron's full transport, with its checkpoints
+// every kSeg events.  With a queue word (buf.queue) the grid is resident and
+// a lane that finishes its electron takes the next from the queue, so that
+// lanes do not idle while the longest trajectory of their warp runs (one
+// thread per electron kept about 18 of 32 lanes busy); without one, each
+// warp takes `range` = 32 consecutive electrons, one per lane.
 template <class T>
 __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const SoftHist sh, const AdjBuf buf,
-                                                 double* hout, mcd_tally* tally, uint32_t* status) {
+                                                 uint32_t range, double* hout, mcd_tally* tally,
+                                                 uint32_t* status) {
     __shared__ SimConst<T> c;  // see k_plain: constants are read from shared memory
     __shared__ double sh_h[MCD_HIST_E_MAX + 2];
     __shared__ unsigned long long s_cnt[9];
@@ -112,44 +120,75 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
     for (int b = threadIdx.x; b < sh.nbins + 2; b += blockDim.x) sh_h[b] = 0.0;
     if (threadIdx.x < 9) s_cnt[threadIdx.x] = 0ull;
     __syncthreads();
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint64_t n = (uint64_t)c.num_el;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint64_t pos = warp * range;
+    const uint64_t end = buf.queue ? n : (pos + range < n ? pos + range : n);
+    bool exhausted = false;
+    const bool depth = sh.quantity == MCD_ADJ_MAX_DEPTH;
+    T* ck = static_cast<T*>(buf.ckpt);
     uint32_t st = 0;
-    if (i < (uint64_t)c.num_el) {
-        const bool depth = sh.quantity == MCD_ADJ_MAX_DEPTH;
-        Lane<T> L;
-        lane_init(L, c);
-        const uint64_t elec = c.first + i;
-        T* ck = static_cast<T*>(buf.ckpt);
-        const size_t n = (size_t)c.num_el;
-        int kstar = -1, mstar = 0;   // exit event; events up to the deepest point
-        T zbest = (T)0;
-        while (L.outcome == MCD_OUT_NONE) {
-            if ((L.step % kSeg) == 0) {
-                const int64_t m = L.step / kSeg;
-                if (m < buf.max_ckpt) {
-                    if (!depth) {
-                        ck[(size_t)m * n + i] = L.E;
-                    } else {
-                        T* q = ck + (size_t)m * kDepthState * n + i;
-                        q[0] = L.E;
-                        q[n] = L.z;
-                        q[2 * n] = L.dx;
-                        q[3 * n] = L.dy;
-                        q[4 * n] = L.dz;
-                        q[5 * n] = L.yx;
-                        q[6 * n] = L.yy;
-                        q[7 * n] = L.yz;
-                    }
+    Lane<T> L;
+    uint64_t i = 0;
+    bool have = false;
+    int kstar = -1, mstar = 0;   // exit event; events up to the deepest point
+    T zbest = (T)0;
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !have);
+        if (idle && !exhausted) {   // the idle lanes take the next electrons
+            const unsigned cnt = (unsigned)__popc(idle);
+            unsigned long long base = pos;
+            if (buf.queue) {
+                if (lane == 0) base = atomicAdd(buf.queue, (unsigned long long)cnt);
+                base = __shfl_sync(0xffffffffu, base, 0);
+            } else {
+                pos += cnt;
+            }
+            const uint64_t j = base + (uint64_t)__popc(idle & lt);
+            if (!have && j < end) {
+                i = j;
+                lane_init(L, c);
+                kstar = -1;
+                mstar = 0;
+                zbest = (T)0;
+                have = true;
+            }
+            if (base + cnt >= end) exhausted = true;
+        }
+        if (__ballot_sync(0xffffffffu, have) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        if (!have) continue;
+        if ((L.step % kSeg) == 0) {
+            const int64_t m = L.step / kSeg;
+            if (m < buf.max_ckpt) {
+                if (!depth) {
+                    ck[(size_t)m * n + i] = L.E;
+                } else {
+                    T* q = ck + (size_t)m * kDepthState * n + i;
+                    q[0] = L.E;
+                    q[n] = L.z;
+                    q[2 * n] = L.dx;
+                    q[3 * n] = L.dy;
+                    q[4 * n] = L.dz;
+                    q[5 * n] = L.yx;
+                    q[6 * n] = L.yy;
+                    q[7 * n] = L.yz;
                 }
             }
-            EventOut<T> ev;
-            cont_event<T, false>(L, c, elec, &ev);
-            if (L.outcome == MCD_OUT_BKS) kstar = (int)(L.step - 1);
-            if (L.max_z > zbest) {
-                zbest = L.max_z;
-                mstar = (int)L.step;
-            }
         }
+        EventOut<T> ev;
+        cont_event<T, false>(L, c, c.first + i, &ev);
+        if (L.outcome == MCD_OUT_BKS) kstar = (int)(L.step - 1);
+        if (L.max_z > zbest) {
+            zbest = L.max_z;
+            mstar = (int)L.step;
+        }
+        if (L.outcome == MCD_OUT_NONE) continue;
+        // the electron is done
         const bool bks = L.outcome == MCD_OUT_BKS;
         const int key = depth ? mstar : kstar;
         if (bks && key > 0 && (key - 1) / kSeg >= buf.max_ckpt) st |= MCD_FLAG_CKPT;
@@ -157,6 +196,8 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
         const T q = depth ? L.max_z : L.E_row;
         static_cast<T*>(buf.E_exit)[i] = q;
         if (bks) {
+            // summed per block in FP64 (straight to the output the clustered
+            // depths contend for a few addresses: 2.3 times slower)
             soft_bins<T>(sh, q, [&](int b, T w, T) { if (w > (T)0) atomicAdd(&sh_h[b], (double)w); });
             atomicAdd(&sh_h[sh.nbins], (double)q);
             atomicAdd(&sh_h[sh.nbins + 1], 1.0);
@@ -166,9 +207,10 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
         if (L.flags & F_CLAMPED) st |= MCD_FLAG_CLAMPED;
         if (L.flags & F_LONG_PATH) st |= MCD_FLAG_LONG_PATH;
         if (L.outcome == MCD_OUT_LONG) st |= MCD_FLAG_LONG;
+        have = false;
     }
     const uint32_t w = __reduce_or_sync(0xffffffffu, st);
-    if ((threadIdx.x & 31) == 0 && w) atomicOr(status, w);
+    if (lane == 0 && w) atomicOr(status, w);
     __syncthreads();
     for (int b = threadIdx.x; b < sh.nbins + 2; b += blockDim.x)
         if (sh_h[b] != 0.0) atomicAdd(&hout[b], sh_h[b]);
@@ -358,7 +400,9 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
     const uint64_t lo = warp * (uint64_t)kBwdRange;
     BksFeed f{lo < n ? lo : n, lo + kBwdRange < n ? lo + kBwdRange : n, 0, 0u};
     const T* ck = static_cast<const T*>(buf.ckpt);
-    double gj = 0.0, gn = 0.0;
+    // the lane's sums over its electrons, in T (a few electrons per lane),
+    // and over the lanes and blocks in FP64
+    T gj = (T)0, gn = (T)0;
     // lane state: its electron, the exit event, the segment to sweep next and
     // (exit energy) the adjoint of E and the electron's parameter sums
     int64_t cur = -1;
@@ -386,8 +430,8 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
         if constexpr (DEPTH) {   // the whole electron in one trip
             T a, b;
             depth_sweep<T>(c, buf, i, elec, ks, lam, ij, ins, &a, &b);
-            gj += (double)a;
-            gn += (double)b;
+            gj += a;
+            gn += b;
             cur = -1;
             continue;
         }
@@ -412,18 +456,19 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
             lam *= (T)1 + s * (dlnsig<T>(c, Ek) * S - SE);
         }
         if (--m < 0) {
-            gj += (double)sj;
-            gn += (double)sn;
+            gj += sj;
+            gn += sn;
             cur = -1;
         }
     }
+    double dj = (double)gj, dn = (double)gn;
     for (int o = 16; o > 0; o >>= 1) {
-        gj += __shfl_down_sync(0xffffffffu, gj, o);
-        gn += __shfl_down_sync(0xffffffffu, gn, o);
+        dj += __shfl_down_sync(0xffffffffu, dj, o);
+        dn += __shfl_down_sync(0xffffffffu, dn, o);
     }
     if (lane == 0) {
-        atomicAdd(&red[0], gj);
-        atomicAdd(&red[1], gn);
+        atomicAdd(&red[0], dj);
+        atomicAdd(&red[1], dn);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -504,6 +549,7 @@ static int adj_args(const mcd_sim* sim, const mcd_material* mat, const mcd_softh
     ab->kstar = buf->kstar;
     ab->E_exit = buf->E_exit;
     ab->max_ckpt = buf->max_ckpt;
+    ab->queue = buf->queue;
     return MCD_OK;
 }
 
@@ -519,16 +565,32 @@ extern "C" int mcd_adjoint_forward(const mcd_sim* sim, const mcd_material* mat, 
     int rc = adj_args(sim, mat, hist, buf, &sh, &ab);
     if (rc != MCD_OK) return rc;
     if (!hist_out || !status) return MCD_EINVAL;
-    const unsigned long long grid = ((unsigned long long)sim->num_el + 255) / 256;
-    if (grid == 0) return MCD_OK;
-    if (grid > 0x7fffffffull) return MCD_ETOOBIG;
+    if (sim->num_el == 0) return MCD_OK;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint32_t range = 32;
+    unsigned long long grid = ((unsigned long long)sim->num_el + 255) / 256;   // one thread per electron
+    if (ab.queue) {
+        // a resident grid: as many blocks as fit on the GPU at once, and no
+        // more than there are electrons for
+        int dev = 0, sms = 0, blocks = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return MCD_ECUDA;
+        const cudaError_t oc = sim->precision == MCD_FP64
+                                   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_adj_fwd<double>, 256, 0)
+                                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_adj_fwd<float>, 256, 0);
+        if (oc != cudaSuccess) return MCD_ECUDA;
+        const unsigned long long resident = (unsigned long long)(sms > 0 ? sms : 1) * (blocks > 0 ? blocks : 1);
+        grid = grid < resident ? grid : resident;
+        if (cudaMemsetAsync(ab.queue, 0, sizeof(unsigned long long), st) != cudaSuccess) return MCD_ECUDA;
+    }
+    if (grid > 0x7fffffffull) return MCD_ETOOBIG;
     if (sim->precision == MCD_FP64)
         k_adj_fwd<double><<<(unsigned)grid, 256, 0, st>>>(make_consts<double>(*sim, *mat, nullptr, nullptr), sh, ab,
-                                                           hist_out, tally, status);
+                                                           range, hist_out, tally, status);
     else
         k_adj_fwd<float><<<(unsigned)grid, 256, 0, st>>>(make_consts<float>(*sim, *mat, nullptr, nullptr), sh, ab,
-                                                          hist_out, tally, status);
+                                                          range, hist_out, tally, status);
     return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
 }
 

@@ -188,7 +188,7 @@ class SoftHist(C.Structure):
 
 class AdjointBuf(C.Structure):
     _fields_ = [("ckpt", C.c_void_p), ("kstar", C.c_void_p), ("E_exit", C.c_void_p), ("max_ckpt", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("queue", C.c_void_p)]
 
 
 STRUCTS = {

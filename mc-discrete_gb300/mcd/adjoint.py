@@ -66,7 +66,9 @@ class ExitEnergyModel:
         self.ckpt = torch.empty(shape, dtype=dt, device=self.device)
         self.kstar = torch.empty(self.n, dtype=torch.int32, device=self.device)
         self.E_exit = torch.empty(self.n, dtype=dt, device=self.device)
-        self.buf = AdjointBuf(self.ckpt.data_ptr(), self.kstar.data_ptr(), self.E_exit.data_ptr(), self.max_ckpt, 0)
+        self.queue = torch.zeros(1, dtype=torch.int64, device=self.device)   # the forward pass's work queue
+        self.buf = AdjointBuf(self.ckpt.data_ptr(), self.kstar.data_ptr(), self.E_exit.data_ptr(), self.max_ckpt, 0,
+                              self.queue.data_ptr())
         self.hout = torch.zeros(self.nbins + 2, dtype=torch.float64, device=self.device)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.grad = torch.zeros(2, dtype=torch.float64, device=self.device)
