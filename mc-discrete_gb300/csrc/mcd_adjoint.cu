@@ -237,15 +237,23 @@ __global__ void __launch_bounds__(256) k_adj_fwd(const SimConst<T> cp, const Sof
 // (the renormalisation of d and y after each rotation is left out: it moves
 // a unit vector by rounding only).  Each segment is recomputed from its
 // checkpoint with the forward's own event code.
+// The adjoints a depth sweep carries from one segment to the one before it,
+// and the electron's parameter sums.
+template <class T>
+struct DepthAdj {
+    T lE, ldx, ldy, ldz, lyx, lyy, lyz, sj, sn;
+};
+
+// Segment m of electron i's depth sweep (the segments run last to first).
 template <class T, class C>
-__device__ __forceinline__ void depth_sweep(const C& c, const AdjBuf& buf, uint64_t i, uint64_t elec, int mstar,
-                                            T g, T ij, T ins, T* gj, T* gn) {
+__device__ __forceinline__ void depth_segment(const C& c, const AdjBuf& buf, uint64_t i, uint64_t elec, int mstar,
+                                              int m, T g, T ij, T ins, DepthAdj<T>& A) {
     const T* ck = static_cast<const T*>(buf.ckpt);
     const size_t n = (size_t)c.num_el;
-    T lE = (T)0, ldx = (T)0, ldy = (T)0, ldz = (T)0, lyx = (T)0, lyy = (T)0, lyz = (T)0;
-    T sj = (T)0, sn = (T)0;
+    T lE = A.lE, ldx = A.ldx, ldy = A.ldy, ldz = A.ldz, lyx = A.lyx, lyy = A.lyy, lyz = A.lyz;
+    T sj = A.sj, sn = A.sn;
     T aE[kSeg], aS[kSeg], aS2[kSeg], aU[kSeg], aP[kSeg], aD[3][kSeg], aY[3][kSeg];
-    for (int m = (mstar - 1) / kSeg; m >= 0; --m) {
+    {
         const int k0 = m * kSeg;
         const int len = min(kSeg, mstar - k0);
         const T* q = ck + (size_t)m * kDepthState * n + i;
@@ -319,8 +327,7 @@ __device__ __forceinline__ void depth_sweep(const C& c, const AdjBuf& buf, uint6
             lyz = nyz;
         }
     }
-    *gj = sj;
-    *gn = sn;
+    A = DepthAdj<T>{lE, ldx, ldy, ldz, lyx, lyy, lyz, sj, sn};
 }
 
 // The backward pass runs only for backscattered electrons, a fraction of
@@ -408,6 +415,7 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
     int64_t cur = -1;
     int ks = 0, m = 0;
     T lam = (T)0, sj = (T)0, sn = (T)0;
+    DepthAdj<T> dA{};   // depth: the adjoints carried between segments
     const T ij = (T)inv_j, ins = (T)inv_ns;
     while (true) {
         const unsigned idle = __ballot_sync(0xffffffffu, cur < 0);
@@ -421,18 +429,20 @@ __global__ void __launch_bounds__(128, 8) k_adj_bwd(const SimConst<T> cp, const 
                 // product of factors 1 + O(1e-2) and each step adds one term
                 lam = exit_adjoint<T>(sh, buf, gh, (uint64_t)e);
                 sj = sn = (T)0;
+                if constexpr (DEPTH) dA = DepthAdj<T>{};
             }
         }
         if (__ballot_sync(0xffffffffu, cur >= 0) == 0u) break;
         if (cur < 0) continue;
         const uint64_t i = (uint64_t)cur;
         const uint64_t elec = c.first + i;
-        if constexpr (DEPTH) {   // the whole electron in one trip
-            T a, b;
-            depth_sweep<T>(c, buf, i, elec, ks, lam, ij, ins, &a, &b);
-            gj += a;
-            gn += b;
-            cur = -1;
+        if constexpr (DEPTH) {   // one segment per trip; lam holds g = dL/dZ
+            depth_segment<T>(c, buf, i, elec, ks, m, lam, ij, ins, dA);
+            if (--m < 0) {
+                gj += dA.sj;
+                gn += dA.sn;
+                cur = -1;
+            }
             continue;
         }
         // exit energy: one 64-event segment per trip, the last one first
