@@ -643,6 +643,14 @@ __device__ __forceinline__ int tab_pick64(const C& c, double E, double U, double
     return MCD_CH_GRYZ0 + (j - 2);
 }
 
+// The trajectory-independent functions of an event's Philox words, when
+// another lane has computed them ahead: ln U of the step's uniform and the
+// azimuth's cos and sin (with the half-phi fold applied).
+template <class T>
+struct EventPre {
+    T ln_y, cph, sph;
+};
+
 // Rutherford sin^2(theta/2) = a U / (a + 1 - U), a = a0 / E
 // (MC/tools/scattering.py:125-152); for the DS event in FP32 with one
 // division as a0 U / (a0 + E (1 - U)).
@@ -663,14 +671,18 @@ __device__ __forceinline__ uint4 event_counter(uint32_t step, uint64_t elec, uin
 // advanced).  Returns the channel code.
 template <class T, bool REC, class C>
 __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r, EventOut<T>* ev,
-                                          bool use_tab = false) {
+                                          bool use_tab = false, const EventPre<T>* pre = nullptr) {
     const T E = L.E;
     int ch = MCD_CH_QUINN;
     T inv_tot;
     // FP64: the azimuth's cos/sin depend on the word alone; computed first,
-    // their FP64 chain overlaps the channel pick's instead of closing the event
+    // their FP64 chain overlaps the channel pick's instead of closing the
+    // event (or given, computed ahead by another lane)
     T cph = (T)0, sph = (T)0;
-    if constexpr (sizeof(T) == 8) azimuth<T>(c, r.w, &cph, &sph);
+    if constexpr (sizeof(T) == 8) {
+        if (pre) cph = pre->cph, sph = pre->sph;
+        else azimuth<T>(c, r.w, &cph, &sph);
+    }
     if (use_tab) {
         if constexpr (sizeof(T) == 4) {
             float Etot;
@@ -723,7 +735,7 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     // steps with mean free path xip_g and marks the electron diffracting
     const bool diff_ev = ch == MCD_CH_DIFF;
     L.flags = diff_ev ? (L.flags | F_DIFFRACTING) : (L.flags & ~F_DIFFRACTING);
-    const T s = -Ops<T>::ln_step_word(r.y) * (diff_ev ? c.xip : inv_tot);
+    const T s = -(pre ? pre->ln_y : Ops<T>::ln_step_word(r.y)) * (diff_ev ? c.xip : inv_tot);
     const T x0 = L.x, y0 = L.y, z0 = L.z;
     lane_move(L, c, s);
     // --- energy loss and polar angle (MC/tools/scattering.py:568-679)

@@ -510,6 +510,82 @@ inline void share_sigma_tables(const mcd_sim* sims, int nsims, const SimConst<do
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// FP64 DS transport of a small run, one warp per two electrons.  Such a run
+// lasts as long as its longest trajectory, one dependent chain of
+// instructions.  The 16 lanes of each half-warp run their electron's events
+// in lockstep (every lane holds the same state) and compute, 16 events
+// ahead and one event per lane, what does not depend on the trajectory: the
+// event's Philox block, ln U of its step uniform and the azimuth's cos and
+// sin (the functions the event itself would call); an event takes them
+// from its lane by shuffles, so the chain no longer carries them.  The
+// trajectories are k_plain's, bit for bit.
+__global__ void __launch_bounds__(32) k_plain_lanes64(const SimConst<double> cp, mcd_tally* tally, const ElOut eo,
+                                                      uint32_t* status) {
+    __shared__ BlockTally bt;
+    __shared__ SimConst<double> c;
+    if (threadIdx.x == 0) c = cp;
+    bt_zero(&bt, 1);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, t = lane & 15, h = lane >> 4;
+    const uint64_t i = (uint64_t)blockIdx.x * 2 + (uint64_t)h;
+    bool active = i < (uint64_t)c.num_el;
+    const uint64_t elec = c.first + i;
+    const uint4 w = event_words(c);   // sim id, Philox key, event limit
+    const bool chan = (c.tally_flags & MCD_TALLY_CHANNELS) != 0;
+    Lane<double> L;
+    lane_init(L, c);
+    uint32_t base = 0, px = 0, pz = 0;
+    double pl = 0.0, pc = 0.0, ps = 0.0;
+    auto ahead = [&]() {   // lane t: the event at step base + t
+        const uint4 r = philox(event_counter(base + (uint32_t)t, elec, w.x), w.y, w.z);
+        px = r.x;
+        pz = r.z;
+        pl = ln_word(r.y);
+        azimuth<double>(c, r.w, &pc, &ps);
+    };
+    ahead();
+    uint32_t st = 0;
+    while (__any_sync(0xffffffffu, active)) {
+        if (active && L.step - base == 16u) {
+            base += 16u;
+            ahead();
+        }
+        const int src = (h << 4) | (int)((L.step - base) & 15u);
+        const uint32_t rx = __shfl_sync(0xffffffffu, px, src);
+        const uint32_t rz = __shfl_sync(0xffffffffu, pz, src);
+        EventPre<double> pre;
+        pre.ln_y = __shfl_sync(0xffffffffu, pl, src);
+        pre.cph = __shfl_sync(0xffffffffu, pc, src);
+        pre.sph = __shfl_sync(0xffffffffu, ps, src);
+        if (!active) continue;
+        if (L.step >= w.w) {   // the 'long' check that opens every event (MC/tools/singleScatter.py:19-23)
+            L.outcome = MCD_OUT_LONG;
+            L.E_row = L.E;
+        } else {
+            L.step += 1;
+            EventOut<double> ev;
+            const int ch = ds_event_r<double, false>(L, c, make_uint4(rx, 0u, rz, 0u), &ev, c.sig != nullptr, &pre);
+            if (chan && t == 0 && ch >= 0) atomicAdd(&bt.channel[ch], 1ull);
+        }
+        if (L.outcome != MCD_OUT_NONE) {
+            if (t == 0) st |= finish_electron(c, L, i, bt, tally, eo);
+            active = false;
+        }
+    }
+    or_status(status, st);
+    __syncthreads();
+    if (threadIdx.x == 0) bt_flush(bt, tally);
+}
+
+static int launch_lanes64(const SimConst<double>& c, mcd_tally* tally, const ElOut& eo, uint32_t* status,
+                          cudaStream_t st) {
+    const unsigned long long grid = ((unsigned long long)c.num_el + 1) / 2;
+    if (grid == 0) return MCD_OK;
+    if (grid > 0x7fffffffull) return MCD_ETOOBIG;
+    k_plain_lanes64<<<(unsigned)grid, 32, 0, st>>>(c, tally, eo, status);
+    return cudaGetLastError() == cudaSuccess ? MCD_OK : MCD_ECUDA;
+}
+
 template <class T, int MODE, bool REC>
 static int launch_plain(const SimConst<T>& c, int block, mcd_tally* tally, const ElOut& eo,
                         const mcd_event_ring& ring, uint32_t* status, cudaStream_t st) {
@@ -540,7 +616,8 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
     if (!sim || !mat || !tally || !status) return MCD_EINVAL;
     const int rc = check_sim(*sim, *mat, moller, gryz);
     if (rc != MCD_OK) return rc;
-    if (block_size <= 0) {
+    const bool automatic = block_size <= 0;
+    if (automatic) {
         // automatic: 128 threads, halved (down to 8) while the grid would
         // leave SMs idle, so that a small job spreads over the GPU: its
         // trajectories are latency chains, and an SM with fewer lanes runs
@@ -583,9 +660,14 @@ extern "C" int mcd_run(const mcd_sim* sim, const mcd_material* mat, const mcd_ta
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const mcd_table* tm = sim->mode == MCD_MODE_DS ? moller : nullptr;
     const mcd_table* tg = sim->mode == MCD_MODE_DS ? gryz : nullptr;
-    if (sim->precision == MCD_FP64)
-        return dispatch_plain<double>(make_consts<double>(*sim, *mat, tm, tg), block_size, tally, eo, rg, rec,
-                                      status, st);
+    if (sim->precision == MCD_FP64) {
+        const SimConst<double> c = make_consts<double>(*sim, *mat, tm, tg);
+        // where the automatic size reached two electrons per warp, a DS run
+        // without an event ring puts the warp's idle lanes to work
+        if (automatic && block_size == 2 && sim->mode == MCD_MODE_DS && !rec)
+            return launch_lanes64(c, tally, eo, status, st);
+        return dispatch_plain<double>(c, block_size, tally, eo, rg, rec, status, st);
+    }
     return dispatch_plain<float>(make_consts<float>(*sim, *mat, tm, tg), block_size, tally, eo, rg, rec, status,
                                  st);
 }

@@ -143,6 +143,24 @@ def test_fp64_table_on_a_range_bounded_by_powers_of_two():
     assert (same & fe_ok).mean() >= 0.99
 
 
+@pytest.mark.parametrize("tabulated", [True, False], ids=["table", "inline"])
+@pytest.mark.parametrize("name", ["si10_ds", "si_film_diff"])
+def test_fp64_small_run_kernel_equals_plain(name, tabulated):
+    """A small FP64 DS run on the automatic block size goes to the kernel
+    whose idle half-warp lanes compute each event's Philox block, step
+    logarithm and azimuth ahead; its rows and tallies equal the plain
+    kernel's (two threads per block) bit for bit."""
+    p = next(c[1] for c in CASES if c[0] == name)
+    a = engine.run(p, num_el=1000, seed=31, precision="fp64", tabulated=tabulated, block_size=0)
+    b = engine.run(p, num_el=1000, seed=31, precision="fp64", tabulated=tabulated, block_size=2)
+    for k in ("outcome", "n_events", "flags"):
+        assert np.array_equal(a.electrons[k], b.electrons[k]), k
+    for k in ("final_E", "dir", "last_pos", "max_z"):      # NaN directions (the reference's quirk) included
+        assert np.array_equal(a.electrons[k], b.electrons[k], equal_nan=True), k
+    for k in ("bks", "abs", "trsm", "trdf", "long", "events", "double_rows"):
+        assert a.tally[k] == b.tally[k], k
+
+
 def test_fp64_table_equals_inline_on_the_small_configuration():
     """The small FP64 configuration (Si 10 keV, 1000 electrons): with the
     table every trajectory matches the inline run's."""
