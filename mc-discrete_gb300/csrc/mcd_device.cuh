@@ -644,11 +644,12 @@ __device__ __forceinline__ int tab_pick64(const C& c, double E, double U, double
 }
 
 // The trajectory-independent functions of an event's Philox words, when
-// another lane has computed them ahead: ln U of the step's uniform and the
-// azimuth's cos and sin (with the half-phi fold applied).
+// another lane has computed them ahead: ln U of the step's uniform, the
+// azimuth's cos and sin (with the half-phi fold applied), the channel
+// pick's uniform, and the Rutherford angle's a0 U and 1 - U.
 template <class T>
 struct EventPre {
-    T ln_y, cph, sph;
+    T ln_y, cph, sph, ux, a0u, uzc;
 };
 
 // Rutherford sin^2(theta/2) = a U / (a + 1 - U), a = a0 / E
@@ -690,7 +691,7 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
             inv_tot = Ops<T>::div(E, (T)Etot);
         } else {
             double mfp;
-            ch = tab_pick64(c, E, Ops<T>::unit(r.x), &mfp);
+            ch = tab_pick64(c, E, pre ? pre->ux : Ops<T>::unit(r.x), &mfp);
             if (ch >= 0) inv_tot = mfp;
             else use_tab = false, ch = MCD_CH_QUINN;   // a threshold inside the cell
         }
@@ -712,7 +713,7 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
         const T cumQ = tot;
         if (c.bits & kBitDiff) tot += c.dS;
         // --- channel (MC/tools/scattering.py:39-59)
-        const T target = Ops<T>::unit(r.x) * tot;
+        const T target = (pre ? pre->ux : Ops<T>::unit(r.x)) * tot;
         T cum = sR;
         if (target <= cum) {
             ch = MCD_CH_RUTH;
@@ -742,7 +743,11 @@ __device__ __forceinline__ int ds_event_r(Lane<T>& L, const C& c, const uint4 r,
     T W, s2;
     if (ch == MCD_CH_RUTH) {
         W = (T)0;
-        s2 = ruth_s2<T>(c, E, r.z);
+        if constexpr (sizeof(T) == 8) {
+            s2 = pre ? pre->a0u * rcp_pos(fma(E, pre->uzc, c.a0)) : ruth_s2<T>(c, E, r.z);
+        } else {
+            s2 = ruth_s2<T>(c, E, r.z);
+        }
     } else if (ch == MCD_CH_QUINN) {
         W = c.Epl;
         s2 = (T)0;

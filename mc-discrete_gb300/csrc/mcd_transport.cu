@@ -515,10 +515,11 @@ inline void share_sigma_tables(const mcd_sim* sims, int nsims, const SimConst<do
 // instructions.  The 16 lanes of each half-warp run their electron's events
 // in lockstep (every lane holds the same state) and compute, 16 events
 // ahead and one event per lane, what does not depend on the trajectory: the
-// event's Philox block, ln U of its step uniform and the azimuth's cos and
-// sin (the functions the event itself would call); an event takes them
-// from its lane by shuffles, so the chain no longer carries them.  The
-// trajectories are k_plain's, bit for bit.
+// event's Philox block, ln U of its step uniform, the azimuth's cos and
+// sin, and the uniforms of the channel pick and the polar angle (the values
+// the event itself would compute); an event takes them from its lane by
+// shuffles, so the chain no longer carries them.  The trajectories are
+// k_plain's, bit for bit.
 __global__ void __launch_bounds__(32) k_plain_lanes64(const SimConst<double> cp, mcd_tally* tally, const ElOut eo,
                                                       uint32_t* status) {
     __shared__ BlockTally bt;
@@ -534,14 +535,16 @@ __global__ void __launch_bounds__(32) k_plain_lanes64(const SimConst<double> cp,
     const bool chan = (c.tally_flags & MCD_TALLY_CHANNELS) != 0;
     Lane<double> L;
     lane_init(L, c);
-    uint32_t base = 0, px = 0, pz = 0;
-    double pl = 0.0, pc = 0.0, ps = 0.0;
+    uint32_t base = 0, pz = 0;
+    EventPre<double> mine{};
     auto ahead = [&]() {   // lane t: the event at step base + t
         const uint4 r = philox(event_counter(base + (uint32_t)t, elec, w.x), w.y, w.z);
-        px = r.x;
         pz = r.z;
-        pl = ln_word(r.y);
-        azimuth<double>(c, r.w, &pc, &ps);
+        mine.ln_y = ln_word(r.y);
+        azimuth<double>(c, r.w, &mine.cph, &mine.sph);
+        mine.ux = Ops<double>::unit(r.x);
+        mine.a0u = c.a0 * Ops<double>::unit(r.z);
+        mine.uzc = Ops<double>::unit_c(r.z);
     };
     ahead();
     uint32_t st = 0;
@@ -551,12 +554,14 @@ __global__ void __launch_bounds__(32) k_plain_lanes64(const SimConst<double> cp,
             ahead();
         }
         const int src = (h << 4) | (int)((L.step - base) & 15u);
-        const uint32_t rx = __shfl_sync(0xffffffffu, px, src);
-        const uint32_t rz = __shfl_sync(0xffffffffu, pz, src);
+        const uint32_t rz = __shfl_sync(0xffffffffu, pz, src);   // the W tables' uniform (inelastic events)
         EventPre<double> pre;
-        pre.ln_y = __shfl_sync(0xffffffffu, pl, src);
-        pre.cph = __shfl_sync(0xffffffffu, pc, src);
-        pre.sph = __shfl_sync(0xffffffffu, ps, src);
+        pre.ln_y = __shfl_sync(0xffffffffu, mine.ln_y, src);
+        pre.cph = __shfl_sync(0xffffffffu, mine.cph, src);
+        pre.sph = __shfl_sync(0xffffffffu, mine.sph, src);
+        pre.ux = __shfl_sync(0xffffffffu, mine.ux, src);
+        pre.a0u = __shfl_sync(0xffffffffu, mine.a0u, src);
+        pre.uzc = __shfl_sync(0xffffffffu, mine.uzc, src);
         if (!active) continue;
         if (L.step >= w.w) {   // the 'long' check that opens every event (MC/tools/singleScatter.py:19-23)
             L.outcome = MCD_OUT_LONG;
@@ -564,7 +569,7 @@ __global__ void __launch_bounds__(32) k_plain_lanes64(const SimConst<double> cp,
         } else {
             L.step += 1;
             EventOut<double> ev;
-            const int ch = ds_event_r<double, false>(L, c, make_uint4(rx, 0u, rz, 0u), &ev, c.sig != nullptr, &pre);
+            const int ch = ds_event_r<double, false>(L, c, make_uint4(0u, 0u, rz, 0u), &ev, c.sig != nullptr, &pre);
             if (chan && t == 0 && ch >= 0) atomicAdd(&bt.channel[ch], 1ull);
         }
         if (L.outcome != MCD_OUT_NONE) {
