@@ -282,8 +282,9 @@ def cfg1_bench(args, dev):
             "gpu_inline_ms": ms_inline, "gpu_fp32_ms": ms32,
             "longest_electron_events": int(g.electrons["n_events"].max()),
             "note": "the launch lasts as long as its longest trajectory, a chain of dependent instructions "
-                    "(FP64 ones the longest); the automatic block size spreads the electrons over the "
-                    "schedulers (blocks of 2, at most one warp per scheduler)",
+                    "(FP64 ones the longest); the automatic size runs two electrons per warp (at most one "
+                    "warp per scheduler), each on a half-warp whose lanes compute the next 16 events' "
+                    "trajectory-independent values (Philox block, step logarithm, azimuth, uniforms)",
             "cpu_1core_s": cpu[1], "cpu_all_cores_s": cpu[os.cpu_count() or 1], "cpu_cores": os.cpu_count() or 1,
             "cpu_timing": "best of 3 on all cores, one run on 1 core",
             "eta_gpu_fp64": g.tally["bks"] / n, "eta_oracle": float(np.mean(c["outcome"] == 1)),
