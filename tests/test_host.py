@@ -278,3 +278,28 @@ def test_c_caller_links_and_runs(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "ok %d" % _lib.ABI_VERSION, (r.returncode, r.stdout)
+
+
+@pytest.mark.parametrize("species", ["Al", "Si", "Cu", "Au"])
+def test_fp64_table_size_rule_matches_the_library(species):
+    """mcd.tables.sigma_table_fits (which decides whether an FP64 run reads
+    a table) and the library's size check agree on both sides of the
+    buffer's limit: mcd_run refuses a table that does not fit with
+    MCD_ETOOBIG before any launch, and otherwise goes on to the next check
+    (here the missing loss tables: MCD_EINVAL)."""
+    from mcd import engine
+    L = _lib.lib()
+    mat = _lib.material(species)
+    buf = (C.c_double * 4)()
+    addr = (C.addressof(buf) + 15) & ~15
+    seen = set()
+    for Emin in (1.0, 5.0, 10.0, 30.0, 50.0, 100.0, 500.0, 1000.0):
+        for E0 in (5000.0, 10000.0, 30000.0, 60000.0, 1e6):
+            s = engine.make_sim(dict(material=species, E0=E0, Emin=Emin, Wc=50.0, mode="DS"), 16,
+                                precision=_lib.FP64)
+            s.sigma_table = addr
+            rc = L.mcd_run(C.byref(s), C.byref(mat), None, None, 1, None, None, 1, 128, None)
+            fits = tables.sigma_table_fits(s, mat)
+            assert rc == (_lib.EINVAL if fits else _lib.ETOOBIG), (species, Emin, E0, rc)
+            seen.add(fits)
+    assert seen == {True, False}
