@@ -11,7 +11,8 @@ field mask selects (the scatter_output columns wanted; 8-byte header plus
 engine.unpack_events turns back into the 8-byte form chunk by chunk).  Two
 rings alternate: while chunk c+1 is being transported, chunk c's records
 are copied to pinned host memory on a second stream, in pieces handed to a
-consumer callback.  A chunk whose events do
+consumer callback; the copy of the next piece runs while the consumer reads
+the current one.  A chunk whose events do
 not fit its ring is re-run with a larger ring; the counter-based random
 stream makes the re-run exact.
 """
@@ -96,6 +97,7 @@ class EventStream:
         cs = torch.cuda.current_stream(self.device)
         done = [torch.cuda.Event() for _ in range(2)]
         freed = [torch.cuda.Event() for _ in range(2)]
+        copied = [torch.cuda.Event() for _ in range(2)]   # the last copy into each host buffer
         t0 = time.perf_counter()
         total_events = 0
         total_bytes = 0
@@ -129,17 +131,25 @@ class EventStream:
                     done[o % 2].record(cs)
                 continue
             nbytes = n * self.rec_bytes
-            off = 0
             ring = self.rings[slot]
-            while off < nbytes:
-                k = min(self.piece, nbytes - off)
-                hb = self.host[(off // self.piece) % 2]
+            pieces = [(off, min(self.piece, nbytes - off)) for off in range(0, nbytes, self.piece)]
+
+            def issue(j):
+                # piece j into host buffer j % 2, whose previous piece the
+                # consumer has already returned from
+                off, k = pieces[j]
                 with torch.cuda.stream(self.copy_stream):
-                    hb[:k].copy_(ring[off:off + k], non_blocking=True)
-                self.copy_stream.synchronize()
+                    self.host[j % 2][:k].copy_(ring[off:off + k], non_blocking=True)
+                    copied[j % 2].record(self.copy_stream)
+
+            if pieces:
+                issue(0)
+            for j, (_, k) in enumerate(pieces):
+                if j + 1 < len(pieces):
+                    issue(j + 1)            # the next piece crosses the link while the consumer reads this one
+                copied[j % 2].synchronize()
                 if consumer is not None:
-                    consumer(hb[:k].numpy().view(self.dtype), c)
-                off += k
+                    consumer(self.host[j % 2][:k].numpy().view(self.dtype), c)
             with torch.cuda.stream(self.copy_stream):
                 freed[slot].record(self.copy_stream)
             total_events += n
