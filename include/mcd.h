@@ -313,7 +313,10 @@ int mcd_build_sigma_table(const mcd_sim* sim, const mcd_material* mat,
  * 16 or a multiple of 32 up to 256, or 0: 128, halved down to 8 while the
  * grid would leave SMs idle, so that a small job spreads over more SMs with
  * fewer lanes each, and for FP64 transport further down to 2 while the grid
- * stays within one warp per scheduler (results do not depend on it).  A DS
+ * stays within one warp per scheduler; there an FP64 DS run without a ring
+ * puts two electrons on each warp, one per half-warp whose lanes compute
+ * the coming events' random numbers and the functions of them that do not
+ * depend on the trajectory (results do not depend on any of this).  A DS
  * simulation with a sigma_table reads its channel cross sections from it.  */
 int mcd_run(const mcd_sim* sim, const mcd_material* mat,
             const mcd_table* moller, const mcd_table* gryz,
