@@ -252,7 +252,11 @@ __device__ __forceinline__ void depth_segment(const C& c, const AdjBuf& buf, uin
     const size_t n = (size_t)c.num_el;
     T lE = A.lE, ldx = A.ldx, ldy = A.ldy, ldz = A.ldz, lyx = A.lyx, lyy = A.lyy, lyz = A.lyz;
     T sj = A.sj, sn = A.sn;
-    T aE[kSeg], aS[kSeg], aS2[kSeg], aU[kSeg], aP[kSeg], aD[3][kSeg], aY[3][kSeg];
+    // the segment's recorded states (E, d and y before each event); the
+    // event's step, polar angle and uniforms are recomputed from its Philox
+    // block in the sweep (the recorded arrays pass through local memory,
+    // and four more of them cost more traffic than the recomputation)
+    T aE[kSeg], aD[3][kSeg], aY[3][kSeg];
     {
         const int k0 = m * kSeg;
         const int len = min(kSeg, mstar - k0);
@@ -277,14 +281,15 @@ __device__ __forceinline__ void depth_segment(const C& c, const AdjBuf& buf, uin
             aY[1][j] = L.yy;
             aY[2][j] = L.yz;
             EventOut<T> ev;
-            cont_event<T, true>(L, c, elec, &ev);
-            aS[j] = ev.pathl;
-            aS2[j] = ev.s2;
-            aU[j] = ev.u_ang;
-            aP[j] = ev.u_phi;
+            cont_event<T, false>(L, c, elec, &ev);
         }
         for (int j = len - 1; j >= 0; --j) {   // reverse sweep
-            const T E = aE[j], s = aS[j], s2 = aS2[j];
+            const T E = aE[j];
+            // the event's step and angles as cont_event_r computed them
+            const uint4 r = philox(event_counter((uint32_t)(k0 + j), elec, c.sim_id), c.key0, c.key1);
+            const T s = -Ops<T>::ln_step_word(r.y) * Ops<T>::div((T)1, sig_ruth<T>(c, E));
+            const T a_r = Ops<T>::div(c.a0, E);
+            const T s2 = Ops<T>::div(a_r * Ops<T>::unit(r.z), a_r + Ops<T>::unit_c(r.z));
             const T dx = aD[0][j], dy = aD[1][j], dz = aD[2][j];
             const T yx = aY[0][j], yy = aY[1][j], yz = aY[2][j];
             T S, SE, Sj;
@@ -292,13 +297,13 @@ __device__ __forceinline__ void depth_segment(const C& c, const AdjBuf& buf, uin
             const T dl = dlnsig<T>(c, E);
             // angles of the event
             T sp, cp;
-            Ops<T>::sincos_pi(aP[j], &sp, &cp);
+            Ops<T>::sincos_pi(Ops<T>::unit(r.w), &sp, &cp);
             if (c.quirks & MCD_Q_HALF_PHI_FOLD) cp = fabs(cp);
             const T cph = (T)1 - (T)2 * sp * sp, sph = (T)2 * sp * cp;
             const T cth = (T)1 - (T)2 * s2;
             const T sth = (T)2 * Ops<T>::sqrt_(s2) * Ops<T>::sqrt_((T)1 - s2);
             // d s2 / dE with s2 = a U / (a + 1 - U), a = a0 / E
-            const T a = Ops<T>::div(c.a0, E), U = aU[j], Uc = (T)1 - U;
+            const T a = a_r, U = Ops<T>::unit(r.z), Uc = (T)1 - U;
             const T den = a + Uc;
             const T ds2 = -Ops<T>::div(a, E) * Ops<T>::div(U * Uc, den * den);
             const T dsth = sth > (T)0 ? Ops<T>::div((T)2 * cth * ds2, sth) : (T)0;
